@@ -1,0 +1,323 @@
+"""bbpp -- Python binding of the GB300-native Bluebottle pressure-Poisson solver.
+
+The solver is the C ABI in include/bbpp.h, implemented in CUDA for sm_103a in
+``libbbpp.so`` (built in-tree by ``build.py``).  This module is a thin ctypes
+layer over that ABI; it never falls back to a CPU implementation.  When the
+library is missing or no GPU is present, calls that need the device raise.
+
+The operator and method mirror the reference's pressure solve
+(src/cuda_solver.cu:38-300, src/solver_kernel.cu): Jacobi PCG on (-A) phi = rhs,
+residual replacement every 50 iterations, solid cells as decoupled rows.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBDIR = os.path.join(_HERE, "_lib")
+LIBPATH = os.path.join(LIBDIR, "libbbpp.so")
+DROPIN_LIBPATH = os.path.join(LIBDIR, "libbbpp_bluebottle.so")
+
+PERIODIC = 0
+NEUMANN = 2
+
+CONVERGED, TINY_RHS, MAX_ITER, NAN, BAD_ARG, CUDA_ERROR, NO_DEVICE, WAIT_TIMEOUT = range(8)
+FP64, FP32_IR = 0, 1
+GUESS_ZERO, GUESS_GIVEN, GUESS_LEARNED = 0, 1, 2
+STOP_REF_RZ, STOP_TRUE_REL = 0, 1
+
+STATUS_NAMES = {0: "converged", 1: "tiny rhs", 2: "max iterations", 3: "nan residual", 4: "bad argument",
+                5: "cuda error", 6: "no device", 7: "device wait timeout"}
+
+
+class BbppError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__("bbpp: %s%s" % (STATUS_NAMES.get(status, status), (": " + msg) if msg else ""))
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("bc", ctypes.c_int * 6)]
+
+    @classmethod
+    def make(cls, nx, ny, nz, dx=None, dy=None, dz=None, bc=(PERIODIC,) * 6):
+        g = cls()
+        g.nx, g.ny, g.nz = nx, ny, nz
+        g.dx = 1.0 / nx if dx is None else dx
+        g.dy = 1.0 / ny if dy is None else dy
+        g.dz = 1.0 / nz if dz is None else dz
+        for i, b in enumerate(bc):
+            g.bc[i] = b
+        return g
+
+    @property
+    def shape(self):
+        return (self.nz, self.ny, self.nx)
+
+    @property
+    def n(self):
+        return self.nx * self.ny * self.nz
+
+    def as_tuple(self):
+        return (self.nx, self.ny, self.nz, self.dx, self.dy, self.dz, tuple(self.bc))
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("guess", ctypes.c_int), ("stop", ctypes.c_int),
+                ("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("replace_every", ctypes.c_int),
+                ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
+                ("net", ctypes.c_void_p), ("prev", ctypes.c_void_p)]
+
+
+class Report(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iters", ctypes.c_int), ("outer", ctypes.c_int),
+                ("replacements", ctypes.c_int), ("bb", ctypes.c_double), ("rz", ctypes.c_double),
+                ("rel_resid", ctypes.c_double), ("true_rel", ctypes.c_double), ("ms", ctypes.c_double),
+                ("guess_ms", ctypes.c_double), ("bytes", ctypes.c_double), ("launches", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class KStat(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("launches", ctypes.c_int), ("ms", ctypes.c_double),
+                ("bytes", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libbbpp.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        raise OSError("libbbpp.so not built (run bluebottle-3.0_gb300/build.py): %s" % LIBPATH)
+    L = ctypes.CDLL(LIBPATH)
+    P, I, D, S = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    sig = {
+        "bbpp_create": (I, [ctypes.POINTER(Grid), ctypes.POINTER(P)]),
+        "bbpp_destroy": (I, [P]),
+        "bbpp_set_stream": (I, [P, P]),
+        "bbpp_default_opts": (None, [ctypes.POINTER(Opts)]),
+        "bbpp_status_str": (ctypes.c_char_p, [I]),
+        "bbpp_last_error": (ctypes.c_char_p, [P]),
+        "bbpp_solve": (I, [P, P, P, P, ctypes.POINTER(Opts), ctypes.POINTER(Report)]),
+        "bbpp_solve_host": (I, [P, P, P, P, ctypes.POINTER(Opts), ctypes.POINTER(Report)]),
+        "bbpp_spmv": (I, [P, P, P, P]),
+        "bbpp_invm": (I, [P, P]),
+        "bbpp_residual": (I, [P, P, P, P, P, ctypes.POINTER(D), ctypes.POINTER(D)]),
+        "bbpp_sphere_mask": (I, [P, D, D, D, I, P, P, P, P, P]),
+        "bbpp_dev_alloc": (I, [S, ctypes.POINTER(P)]),
+        "bbpp_dev_free": (I, [P]),
+        "bbpp_h2d": (I, [P, P, S]),
+        "bbpp_d2h": (I, [P, P, S]),
+        "bbpp_memset": (I, [P, I, S]),
+        "bbpp_sync": (I, []),
+        "bbpp_flush_l2": (I, []),
+        "bbpp_host_alloc": (I, [S, ctypes.POINTER(P)]),
+        "bbpp_host_free": (I, [P]),
+        "bbpp_kernel_stats": (I, [P, P, I, ctypes.POINTER(I)]),
+        "bbpp_set_profiling": (I, [P, I]),
+        "bbpp_rng_uniform": (None, [ctypes.c_ulonglong, ctypes.c_longlong, D, D, P]),
+        "bbpp_rng_gauss": (None, [ctypes.c_ulonglong, ctypes.c_longlong, P]),
+        "bbpp_version": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, DeviceArray):
+        return a.ptr
+    assert isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+def _check(rc, ctx=None, ok=(CONVERGED,)):
+    if rc not in ok:
+        msg = ""
+        try:
+            msg = (lib().bbpp_last_error(ctx) or b"").decode()
+        except Exception:
+            pass
+        raise BbppError(rc, msg)
+    return rc
+
+
+class DeviceArray:
+    """A device allocation made through the C ABI (no torch involved)."""
+
+    def __init__(self, shape, dtype):
+        self.shape = tuple(shape) if not np.isscalar(shape) else (int(shape),)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        p = ctypes.c_void_p()
+        _check(lib().bbpp_dev_alloc(max(self.nbytes, 1), ctypes.byref(p)))
+        self.ptr = p.value
+
+    @classmethod
+    def from_host(cls, a):
+        a = np.ascontiguousarray(a)
+        d = cls(a.shape, a.dtype)
+        d.upload(a)
+        return d
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        assert a.nbytes == self.nbytes
+        _check(lib().bbpp_h2d(self.ptr, a.ctypes.data, self.nbytes))
+
+    def download(self):
+        out = np.empty(self.shape, self.dtype)
+        _check(lib().bbpp_d2h(out.ctypes.data, self.ptr, self.nbytes))
+        return out
+
+    def zero(self):
+        _check(lib().bbpp_memset(self.ptr, 0, self.nbytes))
+
+    def free(self):
+        if self.ptr:
+            lib().bbpp_dev_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def default_opts(**kw):
+    o = Opts()
+    lib().bbpp_default_opts(ctypes.byref(o))
+    for k, v in kw.items():
+        if k == "net" and v is not None and not isinstance(v, int):
+            v = v.handle
+        if k == "prev" and isinstance(v, DeviceArray):
+            v = v.ptr
+        setattr(o, k, v)
+    return o
+
+
+class Solver:
+    """One solver context (device workspace for one grid)."""
+
+    def __init__(self, grid):
+        self.grid = grid
+        h = ctypes.c_void_p()
+        _check(lib().bbpp_create(ctypes.byref(grid), ctypes.byref(h)))
+        self.handle = h.value
+
+    def close(self):
+        if self.handle:
+            lib().bbpp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, rhs, x, mask=None, ok=(CONVERGED,), **kw):
+        """Device-pointer solve; rhs/x/mask are DeviceArrays."""
+        o = default_opts(**kw)
+        rep = Report()
+        rc = lib().bbpp_solve(self.handle, _ptr(mask), _ptr(rhs), _ptr(x), ctypes.byref(o), ctypes.byref(rep))
+        _check(rc, self.handle, ok)
+        return rep
+
+    def solve_host(self, rhs, mask=None, x0=None, ok=(CONVERGED,), **kw):
+        """Host-array solve (copies inside the call); returns (x, report)."""
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros_like(rhs) if x0 is None else np.ascontiguousarray(x0, dtype=np.float64).copy()
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        o = default_opts(**kw)
+        rep = Report()
+        rc = lib().bbpp_solve_host(self.handle, _ptr(m), _ptr(rhs), _ptr(x), ctypes.byref(o), ctypes.byref(rep))
+        _check(rc, self.handle, ok)
+        return x, rep
+
+    def spmv(self, p, Ap, mask=None):
+        _check(lib().bbpp_spmv(self.handle, _ptr(mask), _ptr(p), _ptr(Ap)), self.handle)
+
+    def invm(self, out):
+        _check(lib().bbpp_invm(self.handle, _ptr(out)), self.handle)
+
+    def residual(self, rhs, x, r, mask=None):
+        rr, bb = ctypes.c_double(), ctypes.c_double()
+        _check(lib().bbpp_residual(self.handle, _ptr(mask), _ptr(rhs), _ptr(x), _ptr(r), ctypes.byref(rr),
+                                   ctypes.byref(bb)), self.handle)
+        return rr.value, bb.value
+
+    def sphere_mask(self, centres, radii, out, origin=(0.0, 0.0, 0.0)):
+        c = np.ascontiguousarray(centres, dtype=np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(radii, dtype=np.float64).reshape(-1)
+        cx, cy, cz = [np.ascontiguousarray(c[:, i]) for i in range(3)]
+        _check(lib().bbpp_sphere_mask(self.handle, origin[0], origin[1], origin[2], len(r), _ptr(cx), _ptr(cy),
+                                      _ptr(cz), _ptr(r), _ptr(out)), self.handle)
+
+    def set_profiling(self, on):
+        _check(lib().bbpp_set_profiling(self.handle, 1 if on else 0))
+
+    def kernel_stats(self):
+        arr = (KStat * 32)()
+        n = ctypes.c_int()
+        _check(lib().bbpp_kernel_stats(self.handle, ctypes.cast(arr, ctypes.c_void_p), 32, ctypes.byref(n)))
+        return [(arr[i].name.decode(), arr[i].launches, arr[i].ms, arr[i].bytes) for i in range(min(n.value, 32))]
+
+
+class PinnedArray:
+    """Page-locked host buffer viewed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        self.dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * self.dtype.itemsize
+        p = ctypes.c_void_p()
+        _check(lib().bbpp_host_alloc(max(n, 1), ctypes.byref(p)))
+        self.ptr = p.value
+        buf = (ctypes.c_char * max(n, 1)).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            lib().bbpp_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def rng_uniform(seed, n, lo=0.0, hi=1.0):
+    out = np.empty(int(n), np.float64)
+    lib().bbpp_rng_uniform(seed, int(n), lo, hi, out.ctypes.data)
+    return out
+
+
+def rng_gauss(seed, n):
+    out = np.empty(int(n), np.float64)
+    lib().bbpp_rng_gauss(seed, int(n), out.ctypes.data)
+    return out
+
+
+def flush_l2():
+    _check(lib().bbpp_flush_l2())
+
+
+def sync():
+    _check(lib().bbpp_sync())

@@ -1,0 +1,99 @@
+// bbpp_internal.h -- host-side context shared by the translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/bbpp.h"
+#include "bbpp_dev.cuh"
+
+struct GraphKey {
+  const void *mask = nullptr, *rhs = nullptr, *x = nullptr, *r = nullptr, *p0 = nullptr, *p1 = nullptr,
+             *Ap = nullptr, *st = nullptr;
+  int len = 0, replace_every = 0, elem = 0;
+  bool rr = false;
+  cudaStream_t stream = nullptr;
+  bool operator==(const GraphKey &o) const {
+    return mask == o.mask && rhs == o.rhs && x == o.x && r == o.r && p0 == o.p0 && p1 == o.p1 && Ap == o.Ap &&
+           st == o.st && len == o.len && replace_every == o.replace_every && elem == o.elem && rr == o.rr &&
+           stream == o.stream;
+  }
+};
+
+// One timed kernel launch: events around it, its kind and the iteration
+// (1-based, within its graph or single launch) it belongs to.
+struct KEv {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int kind = 0;
+  int iter = 0;
+  double bytes = 0;  // algorithmic bytes of the launch
+};
+
+enum KernelKind { KK_SEARCH_SPMV = 0, KK_UPDATE, KK_AXPY, KK_RESID, KK_SEARCH_SPMV_F32, KK_UPDATE_F32,
+                  KK_AXPY_F32, KK_RESID_F32, KK_COUNT };
+
+struct GraphCache {
+  GraphKey key;
+  cudaGraphExec_t exec = nullptr;
+  int kernels = 0;          // kernel nodes per launch
+  std::vector<KEv> evs;     // profiling events captured into the graph
+};
+
+struct IrBuffers;   // FP32 inner-sweep workspace (bbpp_ir.cu)
+struct NetWork;     // learned-guess workspace (bbpp_net.cu)
+
+struct bbpp_ctx {
+  bbpp_grid grid{};
+  bbpp::Geo G{};
+  int sms = 1;
+  int kz = 1;          // z planes per stencil CTA
+  dim3 sgrid;          // stencil grid
+  int egrid = 1;       // elementwise grid (1-D)
+  size_t nparts = 0;   // capacity of partials (per sum)
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  bbpp::DevState *st = nullptr;  // [0]: solve, [1]: auxiliary (residual checks)
+  bbpp::DevState *hst = nullptr; // pinned host mirror
+  double *partials = nullptr;
+  double *r = nullptr, *p[2] = {nullptr, nullptr}, *Ap = nullptr;
+  double *hbuf_rhs = nullptr, *hbuf_x = nullptr;
+  uint8_t *hbuf_mask = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<GraphCache> graphs;
+  bool profiling = false;
+  std::vector<KEv> *rec = nullptr;   // when set, launches record events here
+  std::vector<KEv> free_ev;          // event pool
+  int rec_iter = 0;                  // iteration tag for recorded launches
+  double kms[KK_COUNT] = {0};        // accumulated device ms per kind (profiling)
+  long long klaunch[KK_COUNT] = {0}; // launches per kind (profiling)
+  double kbytes[KK_COUNT] = {0};     // algorithmic bytes per kind (profiling)
+  long long launches = 0;            // kernels launched by the last solve
+  std::string err;
+  IrBuffers *ir = nullptr;
+  NetWork *net = nullptr;
+};
+
+void bbpp_record_error(bbpp_ctx *ctx, cudaError_t e, const char *what, int line);
+int bbpp_geo_init(const bbpp_grid *g, bbpp::Geo *G);
+// profiling helpers (bbpp_solver.cu)
+void bbpp_rec_begin(bbpp_ctx *ctx, int kind, double bytes_per_cell);
+void bbpp_rec_end(bbpp_ctx *ctx);
+void bbpp_rec_collect(bbpp_ctx *ctx, std::vector<KEv> &evs, int iters_done, bool release);
+
+template <typename T>
+int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
+                  bbpp::DevState *st, bbpp::DevState *hst, int replace_every, bool confirm, bool rr, int *iters_out);
+template <typename T>
+int bbpp_pcg_init(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, bbpp::DevState *st,
+                  bbpp::DevState *hst, double tol, int stop, int max_iter, bool zero_x);
+
+// FP32-inner / FP64-refinement method (bbpp_ir.cu)
+int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o, bool zero_x,
+                  bbpp_report *rep);
+void bbpp_ir_free(bbpp_ctx *ctx);
+
+// learned initial guess (bbpp_net.cu)
+int bbpp_net_guess(bbpp_ctx *ctx, void *net, const uint8_t *mask, const double *rhs, const double *prev, double *x,
+                   double *ms);
+void bbpp_net_ctx_free(bbpp_ctx *ctx);

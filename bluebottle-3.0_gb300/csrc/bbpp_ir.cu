@@ -1,0 +1,140 @@
+// bbpp_ir.cu -- FP32-inner / FP64 iterative-refinement PCG.
+//
+// Outer loop (FP64): r = rhs - (-A)x, stop when ||r|| <= tol ||rhs||.
+// Inner sweep (FP32 vectors, FP64 dot accumulators across threads and CTAs):
+// Jacobi PCG on (-A)d = r from d = 0 until ||r_d|| <= inner_tol ||r||, then
+// x += d in FP64.  The inner sweeps reuse the FP64 method's kernels
+// instantiated for float.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "bbpp_internal.h"
+#include "bbpp_kernels.cuh"
+
+using namespace bbpp;
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) {                       \
+      bbpp_record_error(ctx, e_, #call, __LINE__); \
+      return BBPP_CUDA_ERROR;                      \
+    }                                              \
+  } while (0)
+
+struct IrBuffers {
+  float *r = nullptr, *d = nullptr, *rd = nullptr, *p[2] = {nullptr, nullptr}, *Ap = nullptr;
+};
+
+void bbpp_ir_free(bbpp_ctx *ctx) {
+  if (!ctx || !ctx->ir) return;
+  IrBuffers *b = ctx->ir;
+  cudaFree(b->r);
+  cudaFree(b->d);
+  cudaFree(b->rd);
+  cudaFree(b->p[0]);
+  cudaFree(b->p[1]);
+  cudaFree(b->Ap);
+  delete b;
+  ctx->ir = nullptr;
+}
+
+// x += d (FP64 accumulation of the FP32 correction)
+__global__ void k_add_correction(const Geo G, double *__restrict__ x, const float *__restrict__ d) {
+  const unsigned int n = (unsigned int)G.n;
+  for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+    x[c] += (double)d[c];
+}
+
+int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o, bool zero_x,
+                  bbpp_report *rep) {
+  const size_t n = (size_t)ctx->G.n;
+  if (!ctx->ir) {
+    IrBuffers *b = new IrBuffers();
+    ctx->ir = b;
+    CK(cudaMalloc(&b->r, sizeof(float) * n));
+    CK(cudaMalloc(&b->d, sizeof(float) * n));
+    CK(cudaMalloc(&b->rd, sizeof(float) * n));
+    CK(cudaMalloc(&b->p[0], sizeof(float) * n));
+    CK(cudaMalloc(&b->p[1], sizeof(float) * n));
+    CK(cudaMalloc(&b->Ap, sizeof(float) * n));
+  }
+  IrBuffers *b = ctx->ir;
+  DevState *st = ctx->st, *hst = ctx->hst;          // outer state
+  DevState *sti = ctx->st + 1, *hsti = ctx->hst + 1;  // inner state
+  if (zero_x) CK(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+  int inner_total = 0, outer = 0;
+  double bb = 0, rr = 0, rz = 0;
+  int status = BBPP_MAX_ITER;
+  const double tol2 = o->tol * o->tol;
+  for (;;) {
+    // outer residual in FP64, rounded to FP32 for the inner right-hand side
+    memset(hst, 0, sizeof(DevState));
+    hst->stop = 1;
+    CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+    {
+      const Geo &G = ctx->G;
+      if (mask)
+        k_resid<double, float, true><<<ctx->sgrid, NT, 0, ctx->stream>>>(G, x, rhs, b->r, mask, st, ctx->partials,
+                                                                         ctx->kz, RES_INIT);
+      else
+        k_resid<double, float, false><<<ctx->sgrid, NT, 0, ctx->stream>>>(G, x, rhs, b->r, mask, st, ctx->partials,
+                                                                          ctx->kz, RES_INIT);
+      CK(cudaGetLastError());
+    }
+    CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    bb = hst->bb;
+    rr = hst->rr;
+    rz = hst->rz;
+    if (bb < 1e-16) {
+      status = BBPP_TINY_RHS;
+      break;
+    }
+    const double rel2 = rr / bb;
+    if (std::isnan(rel2)) {
+      status = BBPP_NAN;
+      break;
+    }
+    const bool conv = (o->stop == BBPP_STOP_REF_RZ) ? (rz <= tol2 * bb) : (rel2 <= tol2);
+    if (conv) {
+      status = BBPP_CONVERGED;
+      break;
+    }
+    if (outer >= o->max_outer || inner_total > o->max_iter) {
+      status = BBPP_MAX_ITER;
+      break;
+    }
+    // inner target: reduce ||r|| by inner_tol, but never below what the outer
+    // tolerance needs (plus a margin for FP32 round-off)
+    double itol = o->inner_tol;
+    const double need = o->tol / std::sqrt(rel2);
+    if (need > itol) itol = std::min(0.5, need * 0.5);
+    int rc = bbpp_pcg_init<float>(ctx, mask, b->r, b->d, b->rd, sti, hsti, itol, 1, o->max_iter, true);
+    if (rc) return rc;
+    float *const p[2] = {b->p[0], b->p[1]};
+    int it = 0;
+    rc = bbpp_pcg_loop<float>(ctx, mask, b->r, b->d, b->rd, p, b->Ap, sti, hsti, o->replace_every, false, true, &it);
+    if (rc) return rc;
+    inner_total += it;
+    outer++;
+    k_add_correction<<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, b->d);
+    CK(cudaGetLastError());
+    if (hsti->done == DONE_NAN) {
+      status = BBPP_NAN;
+      break;
+    }
+  }
+  rep->iters = inner_total;
+  rep->outer = outer;
+  rep->bb = bb;
+  rep->rz = rz;
+  rep->rel_resid = bb > 0 ? std::sqrt(std::max(0.0, rr) / bb) : 0.0;
+  rep->status = status;
+  // bytes: 41 B/cell per inner iteration (FP32 vectors), 25 B/cell per FP64
+  // outer residual (x, rhs, mask in; FP32 r out ~ 21) and 12 B per correction
+  rep->bytes = (double)n * (41.0 * inner_total + 25.0 * (outer + 1) + 12.0 * outer);
+  return 0;
+}

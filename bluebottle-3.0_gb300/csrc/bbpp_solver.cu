@@ -1,0 +1,868 @@
+// bbpp_solver.cu -- host side of the C ABI (include/bbpp.h): context,
+// launch shapes, CUDA-graph chunks of PCG iterations, and the solve loop.
+//
+// The iteration (src/cuda_solver.cu:192-268) runs as a captured graph of
+// `chunk` iterations: [K1, K2] per iteration, with the replacement iteration
+// (q % replace_every == 0) as [K1, x += alpha p, r = rhs - (-A)x].  Kernels
+// return at once when the device state says the solve is done, so the host
+// reads the state only once per chunk.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bbpp.h"
+#include "bbpp_internal.h"
+#include "bbpp_kernels.cuh"
+
+using namespace bbpp;
+
+#define CK(call)                                                    \
+  do {                                                              \
+    cudaError_t e_ = (call);                                        \
+    if (e_ != cudaSuccess) {                                        \
+      bbpp_record_error(ctx, e_, #call, __LINE__);                  \
+      return BBPP_CUDA_ERROR;                                       \
+    }                                                               \
+  } while (0)
+
+static char g_err[512];
+
+void bbpp_record_error(bbpp_ctx *ctx, cudaError_t e, const char *what, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s (%s) at bbpp_solver.cu:%d: %s", cudaGetErrorName(e), cudaGetErrorString(e), line,
+           what);
+  if (ctx) ctx->err = buf;
+  snprintf(g_err, sizeof(g_err), "%s", buf);
+}
+
+// --------------------------------------------------------------- geometry --
+static unsigned long long div_magic(unsigned int d) {
+  if (d <= 1) return 0ull;
+  // ceil(2^64 / d) = floor((2^64 - 1) / d) + 1 for d > 1
+  return (~0ull) / d + 1ull;
+}
+
+int bbpp_geo_init(const bbpp_grid *g, Geo *G) {
+  if (!g || g->nx < 1 || g->ny < 1 || g->nz < 1) return BBPP_BAD_ARG;
+  if (!(g->dx > 0) || !(g->dy > 0) || !(g->dz > 0)) return BBPP_BAD_ARG;
+  for (int f = 0; f < 6; f++)
+    if (g->bc[f] != BBPP_PERIODIC && g->bc[f] != BBPP_NEUMANN) return BBPP_BAD_ARG;
+  if (g->bc[0] != g->bc[1] || g->bc[2] != g->bc[3] || g->bc[4] != g->bc[5]) return BBPP_BAD_ARG;
+  const long long n = (long long)g->nx * g->ny * g->nz;
+  if (n >= (1ll << 31)) return BBPP_BAD_ARG;
+  memset(G, 0, sizeof(*G));
+  G->nx = g->nx;
+  G->ny = g->ny;
+  G->nz = g->nz;
+  G->px = g->bc[0] == BBPP_PERIODIC;
+  G->py = g->bc[2] == BBPP_PERIODIC;
+  G->pz = g->bc[4] == BBPP_PERIODIC;
+  G->n = n;
+  const double idx2 = 1. / (g->dx * g->dx), idy2 = 1. / (g->dy * g->dy), idz2 = 1. / (g->dz * g->dz);
+  G->cx = idx2;
+  G->cy = idy2;
+  G->cz = idz2;
+  const double pfx = -(g->dx * g->dx) / 6., pfy = -(g->dy * g->dy) / 6., pfz = -(g->dz * g->dz) / 6.;
+  for (int wz = 0; wz < 3; wz++)
+    for (int wy = 0; wy < 3; wy++)
+      for (int wx = 0; wx < 3; wx++) {
+        const int cls = wx + 3 * wy + 9 * wz;
+        const int fx = 2 - wx, fy = 2 - wy, fz = 2 - wz;  // faces present
+        // M as in PP_jacobi_init (src/solver_kernel.cu:72-80)
+        const double M = -idx2 * fx - idy2 * fy - idz2 * fz;
+        G->tab[cls] = -M;
+        G->tab[27 + cls] = (M != 0.) ? -1. / M : 0.;
+        // solid row: sum_d idd2 * pf_d * (faces), src/solver_kernel.cu:684-707
+        G->tab[54 + cls] = idx2 * pfx * fx + idy2 * pfy * fy + idz2 * pfz * fz;
+      }
+  G->mx = div_magic((unsigned)g->nx);
+  G->mxy = div_magic((unsigned)(g->nx * g->ny));
+  return 0;
+}
+
+namespace bbpp {
+struct Sphere {
+  double x, y, z, w;
+};
+
+// invM per cell (PP_jacobi_init, src/solver_kernel.cu:26-87)
+__global__ void k_invm(const Geo G, double *invM) {
+  const unsigned int n = (unsigned int)G.n;
+  for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const unsigned int row = fdiv(c, G.mx);
+    const unsigned int k = fdiv(c, G.mxy);
+    const int i = (int)(c - row * (unsigned)G.nx);
+    const int j = (int)(row - k * (unsigned)G.ny);
+    invM[c] = G.tab[27 + wall_class(G, i, j, (int)k)];
+  }
+}
+
+// Sphere phase mask (build_phase, src/particle_kernel.cu:148-253).  One CTA
+// per (sphere, periodic image) walks the image's bounding box and marks the
+// cells whose centre satisfies floor(d/r) < 1.  The mask must be zeroed first.
+// Products and sums use round-to-nearest intrinsics (no FMA contraction) so
+// the result is bit-identical to the host restatement.
+__global__ void k_sphere_mask(const Geo G, double dx, double dy, double dz, double xs, double ys,
+                              double zs, int nimg_x, int nimg_y, int nimg_z,
+                              const Sphere *__restrict__ sph, uint8_t *mask) {
+  const int nimg = nimg_x * nimg_y * nimg_z;
+  const int s = blockIdx.x / nimg;
+  int im = blockIdx.x - s * nimg;
+  const int ox = (nimg_x == 3) ? (im % 3) - 1 : 0;
+  im /= nimg_x;
+  const int oy = (nimg_y == 3) ? (im % 3) - 1 : 0;
+  im /= nimg_y;
+  const int oz = (nimg_z == 3) ? im - 1 : 0;
+  const Sphere S = sph[s];
+  const double irad = 1.0 / S.w;
+  const double X = __dadd_rn(S.x, __dmul_rn((double)ox, __dmul_rn((double)G.nx, dx)));
+  const double Y = __dadd_rn(S.y, __dmul_rn((double)oy, __dmul_rn((double)G.ny, dy)));
+  const double Z = __dadd_rn(S.z, __dmul_rn((double)oz, __dmul_rn((double)G.nz, dz)));
+  int i0 = (int)floor(__ddiv_rn(__dsub_rn(__dsub_rn(X, xs), S.w), dx)) - 1;
+  int i1 = (int)ceil(__ddiv_rn(__dadd_rn(__dsub_rn(X, xs), S.w), dx)) + 1;
+  int j0 = (int)floor(__ddiv_rn(__dsub_rn(__dsub_rn(Y, ys), S.w), dy)) - 1;
+  int j1 = (int)ceil(__ddiv_rn(__dadd_rn(__dsub_rn(Y, ys), S.w), dy)) + 1;
+  int k0 = (int)floor(__ddiv_rn(__dsub_rn(__dsub_rn(Z, zs), S.w), dz)) - 1;
+  int k1 = (int)ceil(__ddiv_rn(__dadd_rn(__dsub_rn(Z, zs), S.w), dz)) + 1;
+  i0 = max(i0, 0); j0 = max(j0, 0); k0 = max(k0, 0);
+  i1 = min(i1, G.nx - 1); j1 = min(j1, G.ny - 1); k1 = min(k1, G.nz - 1);
+  if (i1 < i0 || j1 < j0 || k1 < k0) return;
+  const int bx = i1 - i0 + 1, by = j1 - j0 + 1, bz = k1 - k0 + 1;
+  const int nbox = bx * by * bz;
+  const double Xs = __dsub_rn(X, xs), Ys = __dsub_rn(Y, ys), Zs = __dsub_rn(Z, zs);
+  for (int e = threadIdx.x; e < nbox; e += blockDim.x) {
+    const int li = e % bx, t = e / bx;
+    const int lj = t % by, lk = t / by;
+    const int i = i0 + li, j = j0 + lj, k = k0 + lk;
+    const double xx = __dsub_rn(__dmul_rn((double)(i + 1) - 0.5, dx), Xs);
+    const double yy = __dsub_rn(__dmul_rn((double)(j + 1) - 0.5, dy), Ys);
+    const double zz = __dsub_rn(__dmul_rn((double)(k + 1) - 0.5, dz), Zs);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(xx, xx), __dmul_rn(yy, yy)), __dmul_rn(zz, zz));
+    const double d = __dsqrt_rn(d2);
+    if (floor(__dmul_rn(d, irad)) < 1.0) mask[i + (long long)G.nx * (j + (long long)G.ny * k)] = 1;
+  }
+}
+
+}  // namespace bbpp
+
+// ---------------------------------------------------------------- context --
+static int dev_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+static void stencil_shape(bbpp_ctx *ctx) {
+  const Geo &G = ctx->G;
+  const int gx = (G.nx + TX - 1) / TX, gy = (G.ny + TY - 1) / TY;
+  // enough CTAs for one full wave of resident CTAs, each marching kz planes
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_spmv<double, true>, NT, 0);
+  if (per_sm < 1) per_sm = 1;
+  const long long target = (long long)ctx->sms * per_sm;
+  int nzc = (int)std::max<long long>(1, target / std::max(1, gx * gy));
+  nzc = std::min(nzc, G.nz);
+  int kz = (G.nz + nzc - 1) / nzc;
+  if (kz < 4 && G.nz >= 4) kz = 4;  // keep the halo-plane overhead small
+  nzc = (G.nz + kz - 1) / kz;
+  ctx->kz = kz;
+  ctx->sgrid = dim3(gx, gy, nzc);
+  int per_sm2 = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_update<double, true>, NT, 0);
+  if (per_sm2 < 1) per_sm2 = 1;
+  long long eb = std::min<long long>((G.n + NT - 1) / NT, (long long)ctx->sms * per_sm2);
+  ctx->egrid = (int)std::max<long long>(1, eb);
+}
+
+extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
+  if (!out) return BBPP_BAD_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    snprintf(g_err, sizeof(g_err), "no CUDA device");
+    return BBPP_NO_DEVICE;
+  }
+  bbpp_ctx *ctx = new bbpp_ctx();
+  int rc = bbpp_geo_init(g, &ctx->G);
+  if (rc) {
+    delete ctx;
+    return rc;
+  }
+  ctx->grid = *g;
+  ctx->sms = dev_sms();
+  stencil_shape(ctx);
+  const size_t n = (size_t)ctx->G.n;
+  const size_t nparts = std::max<size_t>((size_t)ctx->sgrid.x * ctx->sgrid.y * ctx->sgrid.z, (size_t)ctx->egrid);
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  ctx->stream = ctx->own_stream;
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->st, sizeof(DevState) * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->partials, sizeof(double) * 3 * nparts);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->r, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->p[0], sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->p[1], sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->Ap, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->hst, sizeof(DevState) * 2);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->st, 0, sizeof(DevState) * 2, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->partials, 0, sizeof(double) * 3 * nparts, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    bbpp_record_error(ctx, e, "bbpp_create", __LINE__);
+    bbpp_destroy(ctx);
+    return BBPP_CUDA_ERROR;
+  }
+  ctx->nparts = nparts;
+  *out = ctx;
+  return BBPP_CONVERGED;
+}
+
+static void drop_graphs(bbpp_ctx *ctx) {
+  for (auto &gc : ctx->graphs) {
+    if (gc.exec) cudaGraphExecDestroy(gc.exec);
+    bbpp_rec_collect(ctx, gc.evs, 0, true);
+  }
+  ctx->graphs.clear();
+}
+
+extern "C" int bbpp_destroy(bbpp_ctx *ctx) {
+  if (!ctx) return BBPP_BAD_ARG;
+  drop_graphs(ctx);
+  bbpp_ir_free(ctx);
+  bbpp_net_ctx_free(ctx);
+  if (ctx->st) cudaFree(ctx->st);
+  if (ctx->partials) cudaFree(ctx->partials);
+  if (ctx->r) cudaFree(ctx->r);
+  if (ctx->p[0]) cudaFree(ctx->p[0]);
+  if (ctx->p[1]) cudaFree(ctx->p[1]);
+  if (ctx->Ap) cudaFree(ctx->Ap);
+  if (ctx->hst) cudaFreeHost(ctx->hst);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (auto &gc : ctx->graphs) bbpp_rec_collect(ctx, gc.evs, 0, true);
+  for (auto &k : ctx->free_ev) {
+    cudaEventDestroy(k.a);
+    cudaEventDestroy(k.b);
+  }
+  if (ctx->hbuf_mask) cudaFree(ctx->hbuf_mask);
+  if (ctx->hbuf_rhs) cudaFree(ctx->hbuf_rhs);
+  if (ctx->hbuf_x) cudaFree(ctx->hbuf_x);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return BBPP_CONVERGED;
+}
+
+extern "C" int bbpp_set_stream(bbpp_ctx *ctx, void *stream) {
+  if (!ctx) return BBPP_BAD_ARG;
+  drop_graphs(ctx);
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return BBPP_CONVERGED;
+}
+
+extern "C" void bbpp_default_opts(bbpp_opts *o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->precision = BBPP_FP64;
+  o->guess = BBPP_GUESS_ZERO;
+  o->stop = BBPP_STOP_TRUE_REL;
+  o->tol = 1e-8;
+  o->max_iter = 20000;
+  o->replace_every = 50;
+  o->inner_tol = 1e-4;
+  o->max_outer = 30;
+  o->net = nullptr;
+  o->prev = nullptr;
+}
+
+extern "C" const char *bbpp_status_str(int s) {
+  switch (s) {
+    case BBPP_CONVERGED: return "converged";
+    case BBPP_TINY_RHS: return "tiny rhs";
+    case BBPP_MAX_ITER: return "max iterations";
+    case BBPP_NAN: return "nan residual";
+    case BBPP_BAD_ARG: return "bad argument";
+    case BBPP_CUDA_ERROR: return "cuda error";
+    case BBPP_NO_DEVICE: return "no device";
+    case BBPP_WAIT_TIMEOUT: return "device wait timeout";
+    default: return "unknown";
+  }
+}
+
+extern "C" const char *bbpp_last_error(const bbpp_ctx *ctx) {
+  if (ctx) return ctx->err.c_str();
+  return g_err;
+}
+
+extern "C" const char *bbpp_version(void) { return "bbpp 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------- launches --
+// All launches go to ctx->stream.  Typed on the vector element.
+template <typename T>
+static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap,
+                               DevState *st) {
+  // bytes/cell: read r, p_old (+ mask), write p_new, Ap
+  bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_SEARCH_SPMV : KK_SEARCH_SPMV_F32, 4.0 * sizeof(T) + (mask ? 1 : 0));
+  if (mask)
+    k_search_spmv<T, true><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, r, pold, pnew, Ap, mask, st, ctx->partials,
+                                                               ctx->kz);
+  else
+    k_search_spmv<T, false><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, r, pold, pnew, Ap, mask, st, ctx->partials,
+                                                                ctx->kz);
+  bbpp_rec_end(ctx);
+}
+
+template <typename T>
+static void launch_update(bbpp_ctx *ctx, T *x, T *r, const T *p, const T *Ap, DevState *st, bool rr) {
+  // bytes/cell: read x, r, p, Ap, write x, r
+  bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_UPDATE : KK_UPDATE_F32, 6.0 * sizeof(T));
+  if (rr)
+    k_update<T, true><<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, r, p, Ap, st, ctx->partials);
+  else
+    k_update<T, false><<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, r, p, Ap, st, ctx->partials);
+  bbpp_rec_end(ctx);
+}
+
+template <typename TXT, typename TR>
+static void launch_resid(bbpp_ctx *ctx, const uint8_t *mask, const TXT *x, const TXT *rhs, TR *r, DevState *st,
+                         int mode) {
+  // bytes/cell: read x, rhs (+ mask), write r
+  bbpp_rec_begin(ctx, sizeof(TXT) == 8 ? KK_RESID : KK_RESID_F32,
+                 (rhs ? 2.0 : 1.0) * sizeof(TXT) + sizeof(TR) + (mask ? 1 : 0));
+  if (mask)
+    k_resid<TXT, TR, true><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, x, rhs, r, mask, st, ctx->partials, ctx->kz,
+                                                               mode);
+  else
+    k_resid<TXT, TR, false><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, x, rhs, r, mask, st, ctx->partials,
+                                                                ctx->kz, mode);
+  bbpp_rec_end(ctx);
+}
+
+template <typename T>
+static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
+                             DevState *st, int q, int replace_every, bool rr) {
+  // q = 1-based iteration number; K1 reads p[(q-1)%2] and writes p[q%2]
+  T *pold = p[(q - 1) & 1], *pnew = p[q & 1];
+  launch_search_spmv<T>(ctx, mask, r, pold, pnew, Ap, st);
+  if (q % replace_every == 0) {
+    bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_AXPY : KK_AXPY_F32, 3.0 * sizeof(T));
+    k_axpy_x<T><<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, pnew, st);
+    bbpp_rec_end(ctx);
+    launch_resid<T, T>(ctx, mask, x, rhs, r, st, RES_ITER);
+  } else {
+    launch_update<T>(ctx, x, r, pnew, Ap, st, rr);
+  }
+}
+
+// Capture (or reuse) the graph of iterations q0+1 .. q0+len for these buffers.
+template <typename T>
+static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
+                           DevState *st, int len, int replace_every, bool rr, cudaGraphExec_t *out) {
+  GraphKey key;
+  key.mask = mask;
+  key.rhs = rhs;
+  key.x = x;
+  key.r = r;
+  key.p0 = p[0];
+  key.p1 = p[1];
+  key.Ap = Ap;
+  key.st = st;
+  key.len = len;
+  key.replace_every = replace_every;
+  key.rr = rr;
+  key.elem = (int)sizeof(T);
+  key.stream = ctx->stream;
+  for (auto &gc : ctx->graphs)
+    if (gc.key == key) {
+      *out = gc.exec;
+      return (int)(&gc - &ctx->graphs[0]);
+    }
+  cudaGraph_t graph = nullptr;
+  bbpp_ctx *c = ctx;
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    bbpp_record_error(c, e, "cudaStreamBeginCapture", __LINE__);
+    return BBPP_CUDA_ERROR;
+  }
+  GraphCache gc;
+  gc.key = key;
+  if (ctx->profiling) ctx->rec = &gc.evs;
+  for (int i = 1; i <= len; i++) {
+    ctx->rec_iter = i;
+    launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, i, replace_every, rr);
+  }
+  ctx->rec = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  if (e != cudaSuccess) {
+    bbpp_record_error(c, e, "cudaStreamEndCapture", __LINE__);
+    return BBPP_CUDA_ERROR;
+  }
+  cudaGraphExec_t exec = nullptr;
+  size_t nnodes = 0;
+  cudaGraphGetNodes(graph, nullptr, &nnodes);
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    bbpp_record_error(c, e, "cudaGraphInstantiate", __LINE__);
+    return BBPP_CUDA_ERROR;
+  }
+  if (ctx->graphs.size() >= 8) {
+    cudaGraphExecDestroy(ctx->graphs.front().exec);
+    bbpp_rec_collect(ctx, ctx->graphs.front().evs, 0, true);
+    ctx->graphs.erase(ctx->graphs.begin());
+  }
+  gc.exec = exec;
+  gc.kernels = (int)(nnodes - 2 * gc.evs.size());
+  ctx->graphs.push_back(gc);
+  *out = exec;
+  return (int)ctx->graphs.size() - 1 + 0 * BBPP_CONVERGED;
+}
+
+static int status_of(int done) {
+  switch (done) {
+    case DONE_CONVERGED: return BBPP_CONVERGED;
+    case DONE_MAX_ITER: return BBPP_MAX_ITER;
+    case DONE_NAN: return BBPP_NAN;
+    case DONE_TINY: return BBPP_TINY_RHS;
+    default: return BBPP_MAX_ITER;
+  }
+}
+
+// Core PCG loop for vectors of type T on a given device state.  Used by the
+// FP64 method directly and by FP32_IR for its inner sweeps.  On entry the
+// state has been initialised by a RES_INIT residual (r, rz, rr, bb set).
+template <typename T>
+int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap, DevState *st,
+                  DevState *hst, int replace_every, bool confirm, bool rr, int *iters_out) {
+  const int chunk = (replace_every % 2 == 0) ? replace_every : 2 * replace_every;
+  // q = completed iterations, read back from the device
+  CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int q = hst->iter;
+  // host-side bound: the device state stops the solve after max_iter + 1
+  // iterations; this only guards against a state that never advances
+  long long rounds = 0;
+  const long long max_rounds = 4ll * (hst->max_iter / 1 + 2) + 64;
+  while (hst->done == RUNNING) {
+    if (++rounds > max_rounds) {
+      bbpp_record_error(ctx, cudaErrorUnknown, "solve loop made no progress", __LINE__);
+      return BBPP_CUDA_ERROR;
+    }
+    const int q0 = q;
+    int gi = -1;
+    std::vector<KEv> single;
+    if (q % chunk == 0) {
+      cudaGraphExec_t exec;
+      gi = get_chunk_graph<T>(ctx, mask, rhs, x, r, p, Ap, st, chunk, replace_every, rr, &exec);
+      if (gi < 0) return BBPP_CUDA_ERROR;
+      CK(cudaGraphLaunch(exec, ctx->stream));
+      ctx->launches += ctx->graphs[gi].kernels;
+    } else {
+      if (ctx->profiling) ctx->rec = &single;
+      ctx->rec_iter = 1;
+      launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, q + 1, replace_every, rr);
+      ctx->rec = nullptr;
+      ctx->launches += ((q + 1) % replace_every == 0) ? 3 : 2;
+      CK(cudaGetLastError());
+    }
+    CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    q = hst->iter;
+    if (ctx->profiling) {
+      if (gi >= 0) bbpp_rec_collect(ctx, ctx->graphs[gi].evs, q - q0, false);
+      else bbpp_rec_collect(ctx, single, q - q0, true);
+    }
+    if (hst->done == DONE_PENDING) {
+      if (!confirm) {
+        hst->done = DONE_CONVERGED;
+        CK(cudaMemcpyAsync(&st->done, &hst->done, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        break;
+      }
+      launch_resid<T, T>(ctx, mask, x, rhs, r, st, RES_CONFIRM);
+      ctx->launches += 1;
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  if (iters_out) *iters_out = q;
+  return 0;
+}
+
+template int bbpp_pcg_loop<double>(bbpp_ctx *, const uint8_t *, const double *, double *, double *, double *const[2],
+                                   double *, DevState *, DevState *, int, bool, bool, int *);
+template int bbpp_pcg_loop<float>(bbpp_ctx *, const uint8_t *, const float *, float *, float *, float *const[2],
+                                  float *, DevState *, DevState *, int, bool, bool, int *);
+
+// Initialise a device state and run r = rhs - (-A)x (RES_INIT) for type T.
+template <typename T>
+int bbpp_pcg_init(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, DevState *st, DevState *hst,
+                  double tol, int stop, int max_iter, bool zero_x) {
+  memset(hst, 0, sizeof(DevState));
+  hst->tol2bb = tol * tol;  // multiplied by (rhs,rhs) inside RES_INIT
+  hst->max_iter = max_iter;
+  hst->stop = stop;
+  hst->first = 1;
+  CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+  if (zero_x) CK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)ctx->G.n, ctx->stream));
+  launch_resid<T, T>(ctx, mask, x, rhs, r, st, RES_INIT);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+template int bbpp_pcg_init<double>(bbpp_ctx *, const uint8_t *, const double *, double *, double *, DevState *,
+                                   DevState *, double, int, int, bool);
+template int bbpp_pcg_init<float>(bbpp_ctx *, const uint8_t *, const float *, float *, float *, DevState *,
+                                  DevState *, double, int, int, bool);
+
+// ------------------------------------------------------------------ solve --
+static int check_opts(const bbpp_opts *o) {
+  if (!o) return BBPP_BAD_ARG;
+  if (o->precision != BBPP_FP64 && o->precision != BBPP_FP32_IR) return BBPP_BAD_ARG;
+  if (o->guess < BBPP_GUESS_ZERO || o->guess > BBPP_GUESS_LEARNED) return BBPP_BAD_ARG;
+  if (o->stop != BBPP_STOP_REF_RZ && o->stop != BBPP_STOP_TRUE_REL) return BBPP_BAD_ARG;
+  if (!(o->tol >= 0) || o->max_iter < 0 || o->replace_every < 1) return BBPP_BAD_ARG;
+  if (o->guess == BBPP_GUESS_LEARNED && !o->net) return BBPP_BAD_ARG;
+  return 0;
+}
+
+static int solve_fp64(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o,
+                      bool zero_x, bbpp_report *rep) {
+  DevState *st = ctx->st, *hst = ctx->hst;
+  int rc = bbpp_pcg_init<double>(ctx, mask, rhs, x, ctx->r, st, hst, o->tol, o->stop, o->max_iter, zero_x);
+  if (rc) return rc;
+  double *const p[2] = {ctx->p[0], ctx->p[1]};
+  int iters = 0;
+  rc = bbpp_pcg_loop<double>(ctx, mask, rhs, x, ctx->r, p, ctx->Ap, st, hst, o->replace_every,
+                             o->stop == BBPP_STOP_TRUE_REL, o->stop == BBPP_STOP_TRUE_REL, &iters);
+  if (rc) return rc;
+  rep->iters = iters;
+  rep->replacements = hst->replacements;
+  rep->bb = hst->bb;
+  rep->rz = hst->rz_last;
+  rep->rel_resid = hst->bb > 0 ? std::sqrt(std::max(0.0, hst->rr) / hst->bb) : 0.0;
+  rep->status = status_of(hst->done);
+  // algorithmic bytes: per iteration 81 (mask) or 80 B/cell; per replacement
+  // x-update 24 + residual 25; init residual 25
+  const double n = (double)ctx->G.n;
+  const double per_it = mask ? 81.0 : 80.0;
+  rep->bytes = n * (per_it * iters + 49.0 * hst->replacements + 25.0);
+  return 0;
+}
+
+// Explicit true relative residual of x (uses ctx->Ap as scratch).
+static int true_rel(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x, double *out) {
+  DevState *st = ctx->st + 1, *hst = ctx->hst + 1;
+  memset(hst, 0, sizeof(DevState));
+  hst->tol2bb = 0.0;
+  hst->stop = 1;
+  CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+  launch_resid<double, double>(ctx, mask, x, rhs, ctx->Ap, st, RES_INIT);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *out = hst->bb > 0 ? std::sqrt(hst->rr / hst->bb) : std::sqrt(hst->rr);
+  return 0;
+}
+
+extern "C" int bbpp_solve(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o,
+                          bbpp_report *rep) {
+  bbpp_report tmp;
+  if (!rep) rep = &tmp;
+  memset(rep, 0, sizeof(*rep));
+  if (!ctx || !rhs || !x) return rep->status = BBPP_BAD_ARG;
+  int rc = check_opts(o);
+  if (rc) return rep->status = rc;
+  ctx->launches = 0;
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  bool zero_x = o->guess == BBPP_GUESS_ZERO;
+  if (o->guess == BBPP_GUESS_LEARNED) {
+    rc = bbpp_net_guess(ctx, o->net, mask, rhs, o->prev, x, &rep->guess_ms);
+    if (rc) return rep->status = rc;
+    zero_x = false;
+  }
+  if (o->precision == BBPP_FP64)
+    rc = solve_fp64(ctx, mask, rhs, x, o, zero_x, rep);
+  else
+    rc = bbpp_solve_ir(ctx, mask, rhs, x, o, zero_x, rep);
+  if (rc) return rep->status = rc;
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  CK(cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  rep->ms = ms;
+  rep->launches = (int)ctx->launches;
+  rc = true_rel(ctx, mask, rhs, x, &rep->true_rel);
+  if (rc) return rep->status = rc;
+  return rep->status;
+}
+
+extern "C" int bbpp_solve_host(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x,
+                               const bbpp_opts *o, bbpp_report *rep) {
+  bbpp_report tmp;
+  if (!rep) rep = &tmp;
+  memset(rep, 0, sizeof(*rep));
+  if (!ctx || !rhs || !x) return rep->status = BBPP_BAD_ARG;
+  const size_t n = (size_t)ctx->G.n;
+  if (!ctx->hbuf_rhs) {
+    CK(cudaMalloc(&ctx->hbuf_rhs, sizeof(double) * n));
+    CK(cudaMalloc(&ctx->hbuf_x, sizeof(double) * n));
+    CK(cudaMalloc(&ctx->hbuf_mask, n));
+  }
+  CK(cudaMemcpyAsync(ctx->hbuf_rhs, rhs, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  if (mask) CK(cudaMemcpyAsync(ctx->hbuf_mask, mask, n, cudaMemcpyHostToDevice, ctx->stream));
+  if (o && o->guess == BBPP_GUESS_GIVEN)
+    CK(cudaMemcpyAsync(ctx->hbuf_x, x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = bbpp_solve(ctx, mask ? ctx->hbuf_mask : nullptr, ctx->hbuf_rhs, ctx->hbuf_x, o, rep);
+  if (rc != BBPP_CONVERGED && rc != BBPP_TINY_RHS && rc != BBPP_MAX_ITER && rc != BBPP_NAN) return rc;
+  CK(cudaMemcpyAsync(x, ctx->hbuf_x, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return rc;
+}
+
+// ------------------------------------------------------- kernel-level ABI --
+extern "C" int bbpp_spmv(bbpp_ctx *ctx, const uint8_t *mask, const double *p, double *Ap) {
+  if (!ctx || !p || !Ap) return BBPP_BAD_ARG;
+  launch_resid<double, double>(ctx, mask, p, nullptr, Ap, ctx->st + 1, RES_PLAIN);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+extern "C" int bbpp_invm(bbpp_ctx *ctx, double *invM) {
+  if (!ctx || !invM) return BBPP_BAD_ARG;
+  k_invm<<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, invM);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+extern "C" int bbpp_residual(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x, double *r,
+                             double *rr, double *bb) {
+  if (!ctx || !rhs || !x || !r) return BBPP_BAD_ARG;
+  DevState *st = ctx->st + 1, *hst = ctx->hst + 1;
+  memset(hst, 0, sizeof(DevState));
+  hst->stop = 1;
+  CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+  launch_resid<double, double>(ctx, mask, x, rhs, r, st, RES_INIT);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (rr) *rr = hst->rr;
+  if (bb) *bb = hst->bb;
+  return 0;
+}
+
+extern "C" int bbpp_sphere_mask(bbpp_ctx *ctx, double xs, double ys, double zs, int nsph, const double *cx,
+                                const double *cy, const double *cz, const double *rad, uint8_t *mask) {
+  if (!ctx || !mask || nsph < 0 || (nsph > 0 && (!cx || !cy || !cz || !rad))) return BBPP_BAD_ARG;
+  CK(cudaMemsetAsync(mask, 0, (size_t)ctx->G.n, ctx->stream));
+  if (nsph == 0) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+  }
+  std::vector<Sphere> h(nsph);
+  for (int s = 0; s < nsph; s++) {
+    if (!(rad[s] > 0)) return BBPP_BAD_ARG;
+    h[s] = Sphere{cx[s], cy[s], cz[s], rad[s]};
+  }
+  Sphere *d = nullptr;
+  CK(cudaMalloc(&d, sizeof(Sphere) * nsph));
+  CK(cudaMemcpyAsync(d, h.data(), sizeof(Sphere) * nsph, cudaMemcpyHostToDevice, ctx->stream));
+  const int ix = ctx->G.px ? 3 : 1, iy = ctx->G.py ? 3 : 1, iz = ctx->G.pz ? 3 : 1;
+  k_sphere_mask<<<nsph * ix * iy * iz, NT, 0, ctx->stream>>>(ctx->G, ctx->grid.dx, ctx->grid.dy, ctx->grid.dz, xs,
+                                                              ys, zs, ix, iy, iz, d, mask);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  CK(e);
+  return 0;
+}
+
+// ---------------------------------------------------------- memory helpers --
+extern "C" int bbpp_dev_alloc(size_t bytes, void **ptr) {
+  bbpp_ctx *ctx = nullptr;
+  if (!ptr) return BBPP_BAD_ARG;
+  CK(cudaMalloc(ptr, bytes ? bytes : 1));
+  return 0;
+}
+extern "C" int bbpp_dev_free(void *ptr) {
+  bbpp_ctx *ctx = nullptr;
+  CK(cudaFree(ptr));
+  return 0;
+}
+extern "C" int bbpp_h2d(void *dst, const void *src, size_t bytes) {
+  bbpp_ctx *ctx = nullptr;
+  CK(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+  return 0;
+}
+extern "C" int bbpp_d2h(void *dst, const void *src, size_t bytes) {
+  bbpp_ctx *ctx = nullptr;
+  CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+  return 0;
+}
+extern "C" int bbpp_memset(void *dst, int value, size_t bytes) {
+  bbpp_ctx *ctx = nullptr;
+  CK(cudaMemset(dst, value, bytes));
+  return 0;
+}
+extern "C" int bbpp_sync(void) {
+  bbpp_ctx *ctx = nullptr;
+  CK(cudaDeviceSynchronize());
+  return 0;
+}
+
+__global__ void k_flush(uint4 *buf, size_t n, unsigned int v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    buf[i] = make_uint4(v, v + 1, v + 2, (unsigned)i);
+}
+
+extern "C" int bbpp_flush_l2(void) {
+  bbpp_ctx *ctx = nullptr;
+  static uint4 *buf = nullptr;
+  static unsigned int v = 0;
+  const size_t bytes = 512ull << 20;  // 4x the 129 MB L2
+  if (!buf) CK(cudaMalloc(&buf, bytes));
+  k_flush<<<1024, 256>>>(buf, bytes / sizeof(uint4), ++v);
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+  return 0;
+}
+
+// ----------------------------------------------------------- kernel stats --
+static const char *kk_name[KK_COUNT] = {"search_spmv", "update", "axpy_x", "resid",
+                                        "search_spmv_f32", "update_f32", "axpy_x_f32", "resid_f32"};
+
+void bbpp_rec_begin(bbpp_ctx *ctx, int kind, double bytes_per_cell) {
+  if (!ctx->rec) return;
+  KEv k;
+  if (!ctx->free_ev.empty()) {
+    k = ctx->free_ev.back();
+    ctx->free_ev.pop_back();
+  } else {
+    cudaEventCreate(&k.a);
+    cudaEventCreate(&k.b);
+  }
+  k.kind = kind;
+  k.iter = ctx->rec_iter;
+  k.bytes = bytes_per_cell * (double)ctx->G.n;
+  cudaEventRecord(k.a, ctx->stream);
+  ctx->rec->push_back(k);
+}
+
+void bbpp_rec_end(bbpp_ctx *ctx) {
+  if (!ctx->rec || ctx->rec->empty()) return;
+  cudaEventRecord(ctx->rec->back().b, ctx->stream);
+}
+
+// Add the device time of the launches that did work (iteration tag <=
+// iters_done; the rest returned at once) and optionally release the events.
+void bbpp_rec_collect(bbpp_ctx *ctx, std::vector<KEv> &evs, int iters_done, bool release) {
+  for (auto &k : evs) {
+    if (k.iter <= iters_done) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, k.a, k.b) == cudaSuccess) {
+        ctx->kms[k.kind] += ms;
+        ctx->klaunch[k.kind] += 1;
+        ctx->kbytes[k.kind] += k.bytes;
+      }
+    }
+  }
+  if (release) {
+    for (auto &k : evs) ctx->free_ev.push_back(k);
+    evs.clear();
+  }
+}
+
+extern "C" int bbpp_set_profiling(bbpp_ctx *ctx, int on) {
+  if (!ctx) return BBPP_BAD_ARG;
+  if ((on != 0) != ctx->profiling) drop_graphs(ctx);
+  ctx->profiling = on != 0;
+  for (int k = 0; k < KK_COUNT; k++) {
+    ctx->kms[k] = 0;
+    ctx->klaunch[k] = 0;
+    ctx->kbytes[k] = 0;
+  }
+  return 0;
+}
+
+extern "C" int bbpp_kernel_stats(bbpp_ctx *ctx, bbpp_kstat *out, int max, int *n) {
+  if (!ctx || !n) return BBPP_BAD_ARG;
+  int k = 0;
+  for (int i = 0; i < KK_COUNT; i++) {
+    if (!ctx->klaunch[i]) continue;
+    if (out && k < max) {
+      memset(&out[k], 0, sizeof(bbpp_kstat));
+      snprintf(out[k].name, sizeof(out[k].name), "%s", kk_name[i]);
+      out[k].launches = (int)ctx->klaunch[i];
+      out[k].ms = ctx->kms[i];
+      out[k].bytes = ctx->kbytes[i];
+    }
+    k++;
+  }
+  *n = k;
+  return 0;
+}
+
+extern "C" int bbpp_host_alloc(size_t bytes, void **ptr) {
+  bbpp_ctx *ctx = nullptr;
+  if (!ptr) return BBPP_BAD_ARG;
+  CK(cudaMallocHost(ptr, bytes ? bytes : 1));
+  return 0;
+}
+
+extern "C" int bbpp_host_free(void *ptr) {
+  bbpp_ctx *ctx = nullptr;
+  CK(cudaFreeHost(ptr));
+  return 0;
+}
+
+// ---------------------------------------------------------------- RNG -----
+// Ranq1 (src/rng.c:28-51), uniform (src/rng.c:78-81), polar Gaussian
+// (src/rng.c:85-107).
+namespace {
+struct Ranq1 {
+  unsigned long long v;
+  explicit Ranq1(unsigned long long seed) {
+    v = 4101842887655102017ULL;
+    v ^= seed;
+    v = next();
+  }
+  unsigned long long next() {
+    v ^= v >> 21;
+    v ^= v << 35;
+    v ^= v >> 4;
+    return v * 2685821657736338717ULL;
+  }
+  double dbl() { return 5.42101086242752217e-20 * (double)next(); }
+};
+}  // namespace
+
+extern "C" void bbpp_rng_uniform(unsigned long long seed, long long n, double lo, double hi, double *out) {
+  Ranq1 g(seed);
+  for (long long i = 0; i < n; i++) out[i] = lo + (hi - lo) * g.dbl();
+}
+
+extern "C" void bbpp_rng_gauss(unsigned long long seed, long long n, double *out) {
+  Ranq1 g(seed);
+  long long i = 0;
+  while (i < n) {
+    double v1, v2, s;
+    do {
+      const double u1 = g.dbl(), u2 = g.dbl();
+      v1 = 2 * u1 - 1;
+      v2 = 2 * u2 - 1;
+      s = v1 * v1 + v2 * v2;
+    } while (s >= 1 || s == 0);
+    const double f = std::sqrt(-2 * std::log(s) / s);
+    out[i++] = v1 * f;
+    if (i < n) out[i++] = v2 * f;
+  }
+}

@@ -1,0 +1,174 @@
+/*
+ * bbpp.h -- C ABI of the GB300-native Bluebottle pressure-Poisson solver.
+ *
+ * The library (libbbpp.so) solves the reference's pressure system
+ *     (-A) phi = rhs
+ * (src/cuda_solver.cu:60-73): (-A) is the cell-centred 7-point Laplacian with
+ * per-direction periodic or homogeneous-Neumann boundaries and the Physalis
+ * phase mask, which turns each solid cell into a decoupled row
+ * (src/solver_kernel.cu:684-707).  The method is the reference's Jacobi PCG
+ * (src/cuda_solver.cu:192-268), with residual replacement every
+ * `replace_every` iterations.
+ *
+ * All arrays are dense, x fastest: c = i + nx*(j + ny*k).  There is no ghost
+ * layer: periodic neighbours wrap on the device and wall faces drop out of the
+ * stencil.  `mask` holds one byte per cell, non-zero for solid (the reference's
+ * `phase > -1`); NULL selects the particle-free operator
+ * (cuda_PP_cg_noparts, src/cuda_solver.cu:573).
+ *
+ * Every pointer argument of bbpp_solve / bbpp_spmv is a device pointer.
+ * bbpp_solve_host takes host pointers and does the copies itself.
+ * No function here calls exit(); errors come back as a bbpp_status.
+ *
+ * The drop-in symbols the Bluebottle time loop calls (cuda_PP_cg,
+ * cuda_PP_cg_noparts, cuda_PP_init_jacobi_preconditioner) live in
+ * libbbpp_bluebottle.so and are declared in bbpp_bluebottle.h.
+ */
+#ifndef BBPP_H
+#define BBPP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Pressure boundary type of a face, as the reference's bc.p{W,E,S,N,B,T}
+ * (src/bluebottle.h:218,242). */
+#define BBPP_PERIODIC 0
+#define BBPP_NEUMANN 2
+
+typedef struct bbpp_grid {
+  int nx, ny, nz;   /* interior cells (dom[rank].Gcc.in, jn, kn) */
+  double dx, dy, dz;
+  int bc[6];        /* W, E, S, N, B, T; each direction periodic on both or Neumann on both */
+} bbpp_grid;
+
+typedef enum bbpp_status {
+  BBPP_CONVERGED = 0,  /* stopping test met */
+  BBPP_TINY_RHS = 1,   /* (rhs,rhs) < 1e-16; x = guess, as src/cuda_solver.cu:180-190 */
+  BBPP_MAX_ITER = 2,   /* iteration limit reached (src/cuda_solver.cu:271-279) */
+  BBPP_NAN = 3,        /* (r,z) became NaN (src/cuda_solver.cu:245-251) */
+  BBPP_BAD_ARG = 4,
+  BBPP_CUDA_ERROR = 5,
+  BBPP_NO_DEVICE = 6,
+  BBPP_WAIT_TIMEOUT = 7 /* a bounded device-side wait gave up */
+} bbpp_status;
+
+typedef enum bbpp_precision {
+  BBPP_FP64 = 0,     /* plain FP64 PCG (the reference's arithmetic) */
+  BBPP_FP32_IR = 1   /* FP32 inner PCG, FP64 residual / solution / dot accumulators */
+} bbpp_precision;
+
+typedef enum bbpp_guess {
+  BBPP_GUESS_ZERO = 0,    /* x0 = 0 (src/solver_kernel.cu:280) */
+  BBPP_GUESS_GIVEN = 1,   /* start from x on entry (warm start) */
+  BBPP_GUESS_LEARNED = 2  /* x0 from the learned network (bbpp_net_*) */
+} bbpp_guess;
+
+typedef enum bbpp_stop {
+  BBPP_STOP_REF_RZ = 0,   /* (r,z) <= tol^2 (rhs,rhs): the reference rule (src/cuda_solver.cu:235) */
+  BBPP_STOP_TRUE_REL = 1  /* ||rhs-(-A)x|| / ||rhs|| <= tol, confirmed with an explicit residual */
+} bbpp_stop;
+
+typedef struct bbpp_opts {
+  int precision;      /* bbpp_precision */
+  int guess;          /* bbpp_guess */
+  int stop;           /* bbpp_stop */
+  double tol;         /* pp_residual (REF_RZ) or relative residual (TRUE_REL) */
+  int max_iter;       /* pp_max_iter; at most max_iter+1 iterations, as the reference */
+  int replace_every;  /* explicit residual every n iterations (50 in the reference) */
+  double inner_tol;   /* FP32_IR: relative residual reduction per refinement sweep */
+  int max_outer;      /* FP32_IR: refinement sweeps */
+  void *net;          /* GUESS_LEARNED: a bbpp_net handle */
+  const double *prev; /* GUESS_LEARNED: previous pressure (device), may be NULL */
+} bbpp_opts;
+
+typedef struct bbpp_report {
+  int status;         /* bbpp_status */
+  int iters;          /* PCG iterations (all inner iterations for FP32_IR) */
+  int outer;          /* FP32_IR refinement sweeps (0 for FP64) */
+  int replacements;   /* explicit residual evaluations */
+  double bb;          /* (rhs, rhs) */
+  double rz;          /* final (r, z) */
+  double rel_resid;   /* final recursive ||r|| / ||rhs|| */
+  double true_rel;    /* ||rhs - (-A)x|| / ||rhs|| computed after the solve */
+  double ms;          /* device time of the solve (CUDA events on the solver stream) */
+  double guess_ms;    /* part of ms spent producing the learned guess */
+  double bytes;       /* algorithmic HBM bytes moved (see the roofline notes) */
+  int launches;       /* kernels launched by the solve (library kernels only) */
+} bbpp_report;
+
+typedef struct bbpp_ctx bbpp_ctx;
+
+/* Context: owns the device workspace for one grid, one CUDA stream. */
+int bbpp_create(const bbpp_grid *g, bbpp_ctx **out);
+int bbpp_destroy(bbpp_ctx *ctx);
+/* Use an external stream (cudaStream_t passed as void*); NULL = own stream. */
+int bbpp_set_stream(bbpp_ctx *ctx, void *stream);
+void bbpp_default_opts(bbpp_opts *o);
+const char *bbpp_status_str(int status);
+/* Last CUDA error text recorded by the context (or "" if none). */
+const char *bbpp_last_error(const bbpp_ctx *ctx);
+
+/* Solve (-A)x = rhs.  mask, rhs, x: device pointers (mask may be NULL). */
+int bbpp_solve(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x,
+               const bbpp_opts *o, bbpp_report *rep);
+/* Same with host pointers; the copies are inside the call. */
+int bbpp_solve_host(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x,
+                    const bbpp_opts *o, bbpp_report *rep);
+
+/* Kernel-level entry points (device pointers), used for parity checks. */
+int bbpp_spmv(bbpp_ctx *ctx, const uint8_t *mask, const double *p, double *Ap);
+int bbpp_invm(bbpp_ctx *ctx, double *invM);
+/* Residual: r = rhs - (-A)x; also returns (r,r) and (rhs,rhs). */
+int bbpp_residual(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x,
+                  double *r, double *rr, double *bb);
+
+/* Phase mask of spheres, on the device (src/particle_kernel.cu:148-253):
+ * cell (i,j,k) is solid when floor(d/r) < 1, d the distance of its centre
+ * ((i+0.5)dx + xs, ...) from a sphere centre; periodic directions also test
+ * the images at +-length.  Sphere arrays are host pointers. */
+int bbpp_sphere_mask(bbpp_ctx *ctx, double xs, double ys, double zs, int nsph,
+                     const double *cx, const double *cy, const double *cz,
+                     const double *rad, uint8_t *mask);
+
+/* Device memory helpers for callers without their own allocator. */
+int bbpp_dev_alloc(size_t bytes, void **ptr);
+int bbpp_dev_free(void *ptr);
+int bbpp_h2d(void *dst, const void *src, size_t bytes);
+int bbpp_d2h(void *dst, const void *src, size_t bytes);
+int bbpp_memset(void *dst, int value, size_t bytes);
+int bbpp_sync(void);
+/* Fill a buffer larger than L2 to evict cached lines between timed runs. */
+int bbpp_flush_l2(void);
+/* Page-locked host memory (for end-to-end timing from pinned buffers). */
+int bbpp_host_alloc(size_t bytes, void **ptr);
+int bbpp_host_free(void *ptr);
+
+/* Per-kernel-kind device time accumulated since bbpp_set_profiling(ctx, 1):
+ * launches that did work, their summed CUDA-event ms and algorithmic bytes.
+ * Kinds: search_spmv, update, axpy_x, resid (and _f32 variants). */
+typedef struct bbpp_kstat {
+  char name[32];
+  int launches;
+  double ms;
+  double bytes;
+} bbpp_kstat;
+int bbpp_kernel_stats(bbpp_ctx *ctx, bbpp_kstat *out, int max, int *n);
+/* Enable (1) or disable (0) per-kernel CUDA-event timing and reset the
+ * counters; events are captured between the kernels of the graphs. */
+int bbpp_set_profiling(bbpp_ctx *ctx, int on);
+
+/* Ranq1 generator (src/rng.c:25-107), for reproducible synthetic inputs. */
+void bbpp_rng_uniform(unsigned long long seed, long long n, double lo, double hi, double *out);
+void bbpp_rng_gauss(unsigned long long seed, long long n, double *out);
+
+/* Library version string. */
+const char *bbpp_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BBPP_H */

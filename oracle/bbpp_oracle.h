@@ -1,0 +1,100 @@
+/*
+ * bbpp_oracle.h -- CPU oracle for the Bluebottle pressure-Poisson solve.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C FP64 restatement of the
+ * reference algorithm.  It is used to check the CUDA path and to time the
+ * CPU baseline.  The product library never links, loads or calls it.
+ *
+ * Parity of this restatement is pinned against the reference's own solver
+ * sources (src/cuda_solver.cu, src/solver_kernel.cu), which are compiled
+ * unmodified for the host by oracle/ref/build_ref.py and run on the same
+ * inputs (tests/test_oracle_vs_ref.py, tests/golden/).
+ *
+ * Layout: dense cell-centred arrays, no ghost layer, index
+ *   c = i + nx*(j + ny*k)   (x fastest; the reference GCC_LOC order,
+ *   src/bluebottle.h:70, with the ghost layer stripped).
+ * System: the reference solves (-A) phi = rhs with rhs = "_rhs_p"
+ * (src/cuda_solver.cu:60-73), so every operator below is (-A), which is
+ * symmetric positive (semi-)definite on the fluid cells.
+ */
+#ifndef BBPP_ORACLE_H
+#define BBPP_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Boundary type per face: 0 = PERIODIC, 2 = NEUMANN (src/bluebottle.h:218,242). */
+typedef struct orc_grid {
+  int nx, ny, nz;
+  double dx, dy, dz;
+  int bc[6]; /* W, E, S, N, B, T */
+} orc_grid;
+
+enum { ORC_STOP_REF_RZ = 0, ORC_STOP_TRUE_REL = 1 };
+enum {
+  ORC_CONVERGED = 0,
+  ORC_TINY_RHS = 1,
+  ORC_MAX_ITER = 2,
+  ORC_NAN = 3,
+  ORC_BAD_ARG = 4
+};
+
+typedef struct orc_pcg_opts {
+  int stop;          /* ORC_STOP_REF_RZ (reference rule) or ORC_STOP_TRUE_REL */
+  double tol;        /* pp_residual for REF_RZ; relative residual for TRUE_REL */
+  int max_iter;      /* pp_max_iter */
+  int replace_every; /* 50 in the reference */
+  int nonzero_guess; /* 0: x0 = 0 (reference); 1: start from x on entry */
+  int trace_len;     /* number of alpha/beta values to record (may be 0) */
+  double *trace_alpha;
+  double *trace_beta;
+} orc_pcg_opts;
+
+typedef struct orc_pcg_result {
+  int status;
+  int iters;
+  double bb;        /* (rhs, rhs) */
+  double rz;        /* last (r, z) */
+  double rr;        /* last (r, r), recursive residual */
+  double true_rel;  /* ||rhs - (-A)x|| / ||rhs|| evaluated after the solve */
+} orc_pcg_result;
+
+/* Ranq1 (Numerical Recipes 3rd ed.), as in src/rng.c:25-51,78-107. */
+typedef struct orc_rng { unsigned long long v; int gphase; double g_v1, g_v2, g_s; } orc_rng;
+void orc_rng_init(orc_rng *g, unsigned long long seed);
+unsigned long long orc_rng_u64(orc_rng *g);
+double orc_rng_dbl(orc_rng *g);
+double orc_rng_gauss(orc_rng *g);
+
+int orc_grid_check(const orc_grid *g);
+void orc_invm(const orc_grid *g, double *invM);
+void orc_spmv(const orc_grid *g, const uint8_t *solid, const double *p, double *Ap);
+double orc_dot(long long n, const double *a, const double *b);
+int orc_pcg(const orc_grid *g, const uint8_t *solid, const double *rhs, double *x,
+            const orc_pcg_opts *o, orc_pcg_result *res);
+double orc_true_rel(const orc_grid *g, const uint8_t *solid, const double *rhs, const double *x);
+
+/* Phase mask of spheres (src/particle_kernel.cu:148-253): cell (i,j,k) is
+ * solid when floor(d/r) < 1 for the distance d of its centre from a sphere
+ * centre; periodic directions use the images at +-length.  Domain origin
+ * (xs, ys, zs).  Writes 1 for solid, 0 for fluid. */
+void orc_sphere_mask(const orc_grid *g, double xs, double ys, double zs, int nsph,
+                     const double *cx, const double *cy, const double *cz,
+                     const double *rad, uint8_t *solid);
+
+/* rhs = -(rho/dt) div(u*) (src/solver_kernel.cu:89-176) from face arrays in
+ * dense layouts u[(i + (nx+1)*(j + ny*k))] (x faces, i = 0..nx), v[i + nx*(j +
+ * (ny+1)*k)] and w[i + nx*(j + ny*k)] with k = 0..nz. */
+void orc_rhs_div(const orc_grid *g, double rho_f, double dt, const double *u,
+                 const double *v, const double *w, double *rhs);
+/* Particle masking of the rhs (src/particle_kernel.cu:1753) followed by
+ * coeffs_refine (src/solver_kernel.cu:212-256). */
+void orc_rhs_mask_refine(const orc_grid *g, const uint8_t *solid, double *rhs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,174 @@
+"""GPU parity of the CUDA path against the CPU oracle, through the C ABI.
+
+Kernel level: (-A)p, invM, residual and the sphere mask on odd, tile-edge and
+tiny grids, periodic seams and Neumann walls, masks touching both.
+Solve level: the FP64 method against the oracle's PCG on the same inputs
+(solutions compared to 1e-10 relative after both reach 1e-13), the reference
+(r,z) stopping rule, error statuses, and the FP32-inner method.
+"""
+import numpy as np
+import pytest
+
+import bbpp
+from bbpp import problems
+
+pytestmark = pytest.mark.gpu
+P, N = bbpp.PERIODIC, bbpp.NEUMANN
+
+SHAPES = [
+    ((5, 7, 3), (P,) * 6),
+    ((17, 40, 9), (P, P, P, P, N, N)),
+    ((33, 33, 33), (N,) * 6),
+    ((32, 8, 16), (P, P, N, N, P, P)),
+    ((64, 24, 12), (N, N, P, P, N, N)),
+    ((1, 9, 4), (P,) * 6),
+]
+
+
+def rand_mask(shape, seed, frac=0.15):
+    rng = np.random.default_rng(seed)
+    return (rng.random(shape) < frac).astype(np.uint8)
+
+
+def to_orc(orc, g):
+    return orc.from_tuple(g.as_tuple())
+
+
+@pytest.fixture(scope="module")
+def lib(bbpp_lib):
+    return bbpp_lib
+
+
+@pytest.mark.parametrize("dims,bc", SHAPES)
+@pytest.mark.parametrize("masked", [False, True])
+def test_spmv_matches_oracle(lib, orc, dims, bc, masked):
+    nx, ny, nz = dims
+    g = bbpp.Grid.make(nx, ny, nz, 1.0 / nx, 1.3 / ny, 0.7 / nz, bc)
+    s = bbpp.Solver(g)
+    rng = np.random.default_rng(nx * 31 + ny)
+    p = rng.normal(size=g.shape)
+    mask = rand_mask(g.shape, nz) if masked else None
+    if masked:
+        p[mask == 1] *= 0.5
+    dp = bbpp.DeviceArray.from_host(p)
+    dA = bbpp.DeviceArray(g.shape, np.float64)
+    dm = bbpp.DeviceArray.from_host(mask) if masked else None
+    s.spmv(dp, dA, dm)
+    got = dA.download()
+    ref = orc.spmv(to_orc(orc, g), p, mask)
+    scale = np.abs(p).max() * max(g.dx, g.dy, g.dz) ** -2 * 6
+    assert np.abs(got - ref).max() <= 1e-14 * scale
+
+
+@pytest.mark.parametrize("dims,bc", SHAPES)
+def test_invm_bit_exact(lib, orc, dims, bc):
+    nx, ny, nz = dims
+    g = bbpp.Grid.make(nx, ny, nz, 1.0 / nx, 1.0 / ny, 1.0 / nz, bc)
+    s = bbpp.Solver(g)
+    d = bbpp.DeviceArray(g.shape, np.float64)
+    s.invm(d)
+    assert np.array_equal(d.download(), orc.invm(to_orc(orc, g)))
+
+
+@pytest.mark.parametrize("n,bc,nsph,rad", [(32, "ppn", 6, 3.5), (45, "ppp", 9, 4.2), (24, "nnn", 3, 5.0),
+                                           (64, "ppn", 40, 4.0)])
+def test_sphere_mask_bit_exact(lib, orc, n, bc, nsph, rad):
+    g = problems.make_grid(n, bc)
+    cents, radii = problems.place_spheres(g, nsph, rad, seed=n)
+    # push one sphere across the periodic seam / close to a wall
+    cents[0, 0] = 0.3 * g.dx
+    s = bbpp.Solver(g)
+    dm = bbpp.DeviceArray(g.shape, np.uint8)
+    s.sphere_mask(cents, radii, dm)
+    got = dm.download()
+    ref = orc.sphere_mask(to_orc(orc, g), cents, radii)
+    assert np.array_equal(got, ref)
+    assert np.array_equal(problems.sphere_mask_host(g, cents, radii), ref)
+    assert got.sum() > 0
+
+
+def test_residual_matches_oracle(lib, orc):
+    g = problems.make_grid(40, "ppn")
+    mask = rand_mask(g.shape, 5, 0.05)
+    rng = np.random.default_rng(7)
+    b, x = rng.normal(size=g.shape), rng.normal(size=g.shape)
+    s = bbpp.Solver(g)
+    db, dx, dr = bbpp.DeviceArray.from_host(b), bbpp.DeviceArray.from_host(x), bbpp.DeviceArray(g.shape, np.float64)
+    dm = bbpp.DeviceArray.from_host(mask)
+    rr, bb = s.residual(db, dx, dr, dm)
+    ref = b - orc.spmv(to_orc(orc, g), x, mask)
+    assert np.abs(dr.download() - ref).max() <= 1e-13 * np.abs(ref).max()
+    assert abs(rr - (ref * ref).sum()) <= 1e-12 * rr
+    assert abs(bb - (b * b).sum()) <= 1e-12 * bb
+
+
+def _solve_pair(orc, name, n, tol, **kw):
+    g, mask, rhs, _ = problems.make_problem(name, n=n)
+    s = bbpp.Solver(g)
+    x, rep = s.solve_host(rhs, mask, tol=tol, **kw)
+    xo, res = orc.pcg(to_orc(orc, g), rhs, mask, tol=tol, stop=kw.get("stop", 1))
+    return g, mask, rhs, x, rep, xo, res
+
+
+@pytest.mark.parametrize("name,n", [("C1", 32), ("C2", 48), ("C4", 40)])
+def test_solve_matches_oracle(lib, orc, name, n):
+    g, mask, rhs, x, rep, xo, res = _solve_pair(orc, name, n, 1e-13)
+    assert rep.status == bbpp.CONVERGED and res["status"] == 0
+    assert rep.true_rel <= 1e-13 * 1.01
+    if mask is None:  # all-periodic, singular: compare modulo the mean
+        x, xo = x - x.mean(), xo - xo.mean()
+    else:
+        assert np.all(x[mask == 1] == 0)
+    err = np.linalg.norm(x - xo) / np.linalg.norm(xo)
+    assert err <= 1e-10, err
+    assert abs(rep.iters - res["iters"]) <= max(2, res["iters"] // 50)
+
+
+def test_reference_stop_rule(lib, orc):
+    """(r,z) <= pp_residual^2 (rhs,rhs) (src/cuda_solver.cu:235)."""
+    g, mask, rhs, x, rep, xo, res = _solve_pair(orc, "C2", 32, 1e-6, stop=bbpp.STOP_REF_RZ)
+    assert rep.status == bbpp.CONVERGED
+    assert rep.rz <= 1e-12 * rep.bb
+    assert abs(rep.iters - res["iters"]) <= 1
+    assert np.linalg.norm(x - xo) <= 1e-8 * np.linalg.norm(xo)
+
+
+def test_status_codes(lib):
+    g = problems.make_grid(24, "ppn")
+    s = bbpp.Solver(g)
+    rhs = problems.uniform_rhs(g.shape, 3)
+    x, rep = s.solve_host(rhs, tol=1e-14, max_iter=5, ok=(bbpp.MAX_ITER,))
+    assert rep.status == bbpp.MAX_ITER and rep.iters == 6
+    x, rep = s.solve_host(np.zeros(g.shape), ok=(bbpp.TINY_RHS,))
+    assert rep.status == bbpp.TINY_RHS and rep.iters == 0
+    bad = rhs.copy()
+    bad[3, 4, 5] = np.nan
+    x, rep = s.solve_host(bad, ok=(bbpp.NAN, bbpp.TINY_RHS, bbpp.MAX_ITER))
+    assert rep.status in (bbpp.NAN, bbpp.TINY_RHS)
+    with pytest.raises(bbpp.BbppError):
+        s.solve_host(rhs, tol=-1.0)
+
+
+def test_warm_start_and_repeat(lib, orc):
+    g, mask, rhs, _ = problems.make_problem("C2", n=40)
+    s = bbpp.Solver(g)
+    x1, r1 = s.solve_host(rhs, mask, tol=1e-10)
+    x2, r2 = s.solve_host(rhs, mask, tol=1e-10)
+    assert r1.iters == r2.iters and np.array_equal(x1, x2)  # deterministic reductions
+    x3, r3 = s.solve_host(rhs, mask, x0=x1, tol=1e-10, guess=bbpp.GUESS_GIVEN)
+    assert r3.status == bbpp.CONVERGED and r3.iters <= 1
+
+
+@pytest.mark.parametrize("name,n,tol", [("C2", 64, 1e-8), ("C3", 96, 1e-8), ("C1", 32, 1e-10)])
+def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol):
+    g, mask, rhs, _ = problems.make_problem(name, n=n)
+    s = bbpp.Solver(g)
+    x, rep = s.solve_host(rhs, mask, tol=tol, precision=bbpp.FP32_IR)
+    assert rep.status == bbpp.CONVERGED and rep.true_rel <= tol * 1.01
+    assert rep.outer >= 1
+    xo, res = orc.pcg(to_orc(orc, g), rhs, mask, tol=1e-13)
+    if mask is None:
+        x, xo = x - x.mean(), xo - xo.mean()
+    err = np.abs(x - xo).max() / np.abs(xo).max()
+    # the solution error is bounded by the residual times the condition number
+    assert err < 1e4 * tol, err
