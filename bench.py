@@ -198,11 +198,18 @@ def run_ours(args):
             rep = step(kw)
             assert rep.status == bbpp.CONVERGED, (name, rep.as_dict())
 
+    if args.only:
+        # solves only (for profiler runs): warm-up + steps of one method
+        for _ in range(args.steps):
+            rep = step(methods[args.only])
+            assert rep.status == bbpp.CONVERGED
+        print(json.dumps({"only": args.only, "iters": rep.iters, "ms": rep.ms}))
+        return
+
     res = {}
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     for name, kw in methods.items():
-        s.set_profiling(True)
         reps = []
         barrier()
         bbpp.sync()
@@ -212,14 +219,20 @@ def run_ours(args):
         bbpp.sync()
         wall = time.perf_counter() - t0
         barrier()
-        ks = s.kernel_stats()
-        s.set_profiling(False)
         ms = float(np.mean([r.ms for r in reps]))
         ms = vmax(ms)
         res[name] = dict(ms=ms, iters=reps[-1].iters, outer=reps[-1].outer, true_rel=reps[-1].true_rel,
-                         bytes=reps[-1].bytes, launches=int(sum(r.launches for r in reps)), kstats=ks,
-                         wall_s=wall, status=[r.status for r in reps])
+                         bytes=reps[-1].bytes, launches=int(sum(r.launches for r in reps)),
+                         wall_s=wall, status=[r.status for r in reps], all_ms=[r.ms for r in reps])
     clk = clocks.stop()
+    # per-kernel device time: the same solves again with CUDA events around
+    # every kernel on the solver stream (direct launches instead of graphs)
+    for name, kw in methods.items():
+        s.set_profiling(True)
+        for _ in range(max(1, min(args.steps, 2))):
+            step(kw)
+        res[name]["kstats"] = s.kernel_stats()
+        s.set_profiling(False)
 
     # end to end: host (pinned) buffers in, solution out, copies inside the timed call
     hr = bbpp.PinnedArray(g.shape, np.float64)
@@ -306,6 +319,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--only", default=None, choices=["fp64", "ir"],
+                    help="run only warm-up + steps solves of one method (profiler runs)")
     ap.add_argument("--ref-iters", type=int, default=0,
                     help="iterations of a full solve for the reference arm (0: the measured C3 count)")
     args = ap.parse_args()

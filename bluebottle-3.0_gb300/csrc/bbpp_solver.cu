@@ -392,7 +392,7 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   }
   GraphCache gc;
   gc.key = key;
-  if (ctx->profiling) ctx->rec = &gc.evs;
+  ctx->rec = nullptr;  // graphs carry no profiling events
   for (int i = 1; i <= len; i++) {
     ctx->rec_iter = i;
     launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, i, replace_every, rr);
@@ -457,7 +457,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
     const int q0 = q;
     int gi = -1;
     std::vector<KEv> single;
-    if (q % chunk == 0) {
+    if (q % chunk == 0 && !ctx->profiling) {
       cudaGraphExec_t exec;
       gi = get_chunk_graph<T>(ctx, mask, rhs, x, r, p, Ap, st, chunk, replace_every, rr, &exec);
       if (gi < 0) return BBPP_CUDA_ERROR;
@@ -772,6 +772,8 @@ void bbpp_rec_collect(bbpp_ctx *ctx, std::vector<KEv> &evs, int iters_done, bool
         ctx->kms[k.kind] += ms;
         ctx->klaunch[k.kind] += 1;
         ctx->kbytes[k.kind] += k.bytes;
+      } else {
+        (void)cudaGetLastError();  // timing is best effort; never leak its error
       }
     }
   }
