@@ -193,18 +193,18 @@ def run_ours(args):
         bbpp.flush_l2()
         return s.solve(drhs, dx, dmask, tol=tol, **kw)
 
-    for name, kw in methods.items():
-        for _ in range(args.warmup):
-            rep = step(kw)
-            assert rep.status == bbpp.CONVERGED, (name, rep.as_dict())
-
     if args.only:
-        # solves only (for profiler runs): warm-up + steps of one method
+        # solves of one method only (profiler runs): steps solves, no warm-up
         for _ in range(args.steps):
             rep = step(methods[args.only])
             assert rep.status == bbpp.CONVERGED
         print(json.dumps({"only": args.only, "iters": rep.iters, "ms": rep.ms}))
         return
+
+    for name, kw in methods.items():
+        for _ in range(args.warmup):
+            rep = step(kw)
+            assert rep.status == bbpp.CONVERGED, (name, rep.as_dict())
 
     res = {}
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))

@@ -1,0 +1,323 @@
+// bbpp_bluebottle.cu -- the drop-in entry points of include/bbpp_bluebottle.h.
+//
+// The reference solve (src/cuda_solver.cu:38-300) does, per call: zero
+// _rhs_p; PP_rhs; [particles] cuda_part_BC_p, exchange, coeffs_refine, zero
+// ghosts; (rhs,rhs); PP_cg_init; the PCG loop; recorder_PP.  Here the rhs
+// build and coeffs_refine are two kernels that read the reference's s3b face
+// and cell arrays directly, the PCG runs in libbbpp on dense workspaces, and
+// the solution is written back into _phi's interior.
+#include <cuda_runtime.h>
+#include <sys/time.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#define BBPP_BLUEBOTTLE_IMPL
+#include "../../include/bbpp.h"
+#include "../../include/bbpp_bluebottle.h"
+
+extern "C" bb_bc_pressure bc;  // leading members of the host program's BC
+
+namespace {
+
+struct DropIn {
+  bbpp_ctx *ctx = nullptr;
+  int nx = 0, ny = 0, nz = 0;
+  double dx = 0, dy = 0, dz = 0;
+  int bcs[6] = {0, 0, 0, 0, 0, 0};
+  uint8_t *mask = nullptr;  // dense, one byte per cell
+  double *b = nullptr, *x = nullptr;
+  bool mask_valid = false;
+};
+DropIn g;
+
+void fail(const char *what, int rc) {
+  fprintf(stderr, "N%d >> bbpp pressure solver: %s failed (%s): %s\n", rank, what, bbpp_status_str(rc),
+          bbpp_last_error(g.ctx));
+  exit(EXIT_FAILURE);
+}
+
+void ensure_ctx() {
+  if (nprocs != 1) {
+    fprintf(stderr, "N%d >> bbpp pressure solver: one rank per GPU only (nprocs = %d)\n", rank, nprocs);
+    exit(EXIT_FAILURE);
+  }
+  const bb_dom_struct &d = dom[rank];
+  const int b6[6] = {bc.pW, bc.pE, bc.pS, bc.pN, bc.pB, bc.pT};
+  bool same = g.ctx && g.nx == d.Gcc.in && g.ny == d.Gcc.jn && g.nz == d.Gcc.kn && g.dx == d.dx && g.dy == d.dy &&
+              g.dz == d.dz && memcmp(g.bcs, b6, sizeof(b6)) == 0;
+  if (same) return;
+  bbpp_bluebottle_release();
+  bbpp_grid gr;
+  gr.nx = d.Gcc.in;
+  gr.ny = d.Gcc.jn;
+  gr.nz = d.Gcc.kn;
+  gr.dx = d.dx;
+  gr.dy = d.dy;
+  gr.dz = d.dz;
+  memcpy(gr.bc, b6, sizeof(b6));
+  int rc = bbpp_create(&gr, &g.ctx);
+  if (rc) fail("bbpp_create", rc);
+  g.nx = gr.nx;
+  g.ny = gr.ny;
+  g.nz = gr.nz;
+  g.dx = gr.dx;
+  g.dy = gr.dy;
+  g.dz = gr.dz;
+  memcpy(g.bcs, b6, sizeof(b6));
+  const size_t n = (size_t)gr.nx * gr.ny * gr.nz;
+  if (cudaMalloc(&g.mask, n) != cudaSuccess || cudaMalloc(&g.b, n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&g.x, n * sizeof(double)) != cudaSuccess)
+    fail("workspace allocation", BBPP_CUDA_ERROR);
+  g.mask_valid = false;
+}
+
+// Reference s3b index of interior cell (i, j, k) (0-based), GCC_LOC
+// (src/bluebottle.h:70) with DOM_BUF = 1.
+__device__ __forceinline__ long long gcc_b(int i, int j, int k, int s1b, int s2b) {
+  return (long long)(i + 1) + (long long)(j + 1) * s1b + (long long)(k + 1) * s2b;
+}
+
+struct Shape {
+  int nx, ny, nz;
+  int s1b, s2b;                  // Gcc s1b, s2b
+  int fx_s1b, fx_s2b;            // Gfx: GFX_LOC = j + k s1b + i s2b
+  int fy_s1b, fy_s2b;            // Gfy: GFY_LOC = k + i s1b + j s2b
+  int fz_s1b, fz_s2b;            // Gfz: GFZ_LOC = i + j s1b + k s2b
+  int px, py, pz;
+  double idx, idy, idz, idx2, idy2, idz2;
+};
+
+// mask = (_phase > -1) on the interior
+__global__ void k_mask_from_phase(Shape S, const int *__restrict__ phase, uint8_t *__restrict__ mask) {
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % S.nx);
+    const long long r = c / S.nx;
+    const int j = (int)(r % S.ny), k = (int)(r / S.ny);
+    mask[c] = phase[gcc_b(i, j, k, S.s1b, S.s2b)] > -1;
+  }
+}
+
+// PP_rhs (src/solver_kernel.cu:152-173): rhs = -(rho/dt) div u* on the
+// interior of _rhs_p (ghosts left zero, as after the reference's memset).
+__global__ void k_rhs_div_b(Shape S, double rho_idt, const double *__restrict__ u, const double *__restrict__ v,
+                            const double *__restrict__ w, double *__restrict__ rhs_b) {
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % S.nx);
+    const long long r = c / S.nx;
+    const int j = (int)(r % S.ny), k = (int)(r / S.ny);
+    const int TI = i + 1, TJ = j + 1, TK = k + 1;
+    const double uw = u[TJ + (long long)TK * S.fx_s1b + (long long)TI * S.fx_s2b];
+    const double ue = u[TJ + (long long)TK * S.fx_s1b + (long long)(TI + 1) * S.fx_s2b];
+    const double vs = v[TK + (long long)TI * S.fy_s1b + (long long)TJ * S.fy_s2b];
+    const double vn = v[TK + (long long)TI * S.fy_s1b + (long long)(TJ + 1) * S.fy_s2b];
+    const double wb = w[TI + (long long)TJ * S.fz_s1b + (long long)TK * S.fz_s2b];
+    const double wt = w[TI + (long long)TJ * S.fz_s1b + (long long)(TK + 1) * S.fz_s2b];
+    double s = __dmul_rn(__dsub_rn(ue, uw), S.idx);
+    s = __dadd_rn(s, __dmul_rn(__dsub_rn(vn, vs), S.idy));
+    s = __dadd_rn(s, __dmul_rn(__dsub_rn(wt, wb), S.idz));
+    s = __dmul_rn(s, rho_idt);
+    rhs_b[gcc_b(i, j, k, S.s1b, S.s2b)] = -s;
+  }
+}
+
+// coeffs_refine (src/solver_kernel.cu:212-256) on the s3b rhs, then the dense
+// copy the solver works on.  Periodic neighbours wrap (the reference
+// exchanges rhs first); a wall neighbour adds nothing (its phase ghost is -1).
+__global__ void k_refine_pack(Shape S, const double *__restrict__ rhs_b, const uint8_t *__restrict__ mask,
+                              double *__restrict__ b) {
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % S.nx);
+    const long long r = c / S.nx;
+    const int j = (int)(r % S.ny), k = (int)(r / S.ny);
+    double acc = rhs_b[gcc_b(i, j, k, S.s1b, S.s2b)];
+    if (mask && !mask[c]) {
+      const int ie = (i + 1 < S.nx) ? i + 1 : (S.px ? 0 : -1);
+      const int iw = (i > 0) ? i - 1 : (S.px ? S.nx - 1 : -1);
+      const int jn = (j + 1 < S.ny) ? j + 1 : (S.py ? 0 : -1);
+      const int js = (j > 0) ? j - 1 : (S.py ? S.ny - 1 : -1);
+      const int kt = (k + 1 < S.nz) ? k + 1 : (S.pz ? 0 : -1);
+      const int kb = (k > 0) ? k - 1 : (S.pz ? S.nz - 1 : -1);
+      const long long sy = S.nx, sz = (long long)S.nx * S.ny;
+      if (ie >= 0 && mask[ie + j * sy + k * sz]) acc = __dadd_rn(acc, __dmul_rn(S.idx2, -rhs_b[gcc_b(ie, j, k, S.s1b, S.s2b)]));
+      if (iw >= 0 && mask[iw + j * sy + k * sz]) acc = __dadd_rn(acc, __dmul_rn(S.idx2, -rhs_b[gcc_b(iw, j, k, S.s1b, S.s2b)]));
+      if (jn >= 0 && mask[i + jn * sy + k * sz]) acc = __dadd_rn(acc, __dmul_rn(S.idy2, -rhs_b[gcc_b(i, jn, k, S.s1b, S.s2b)]));
+      if (js >= 0 && mask[i + js * sy + k * sz]) acc = __dadd_rn(acc, __dmul_rn(S.idy2, -rhs_b[gcc_b(i, js, k, S.s1b, S.s2b)]));
+      if (kt >= 0 && mask[i + j * sy + kt * sz]) acc = __dadd_rn(acc, __dmul_rn(S.idz2, -rhs_b[gcc_b(i, j, kt, S.s1b, S.s2b)]));
+      if (kb >= 0 && mask[i + j * sy + kb * sz]) acc = __dadd_rn(acc, __dmul_rn(S.idz2, -rhs_b[gcc_b(i, j, kb, S.s1b, S.s2b)]));
+    }
+    b[c] = acc;
+  }
+}
+
+// _phi interior = x (ghosts are the caller's, src/bluebottle.c:233-234)
+__global__ void k_unpack_phi(Shape S, const double *__restrict__ x, double *__restrict__ phi_b) {
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % S.nx);
+    const long long r = c / S.nx;
+    const int j = (int)(r % S.ny), k = (int)(r / S.ny);
+    phi_b[gcc_b(i, j, k, S.s1b, S.s2b)] = x[c];
+  }
+}
+
+Shape shape_of(const bb_dom_struct &d) {
+  Shape S;
+  S.nx = d.Gcc.in;
+  S.ny = d.Gcc.jn;
+  S.nz = d.Gcc.kn;
+  S.s1b = d.Gcc.s1b;
+  S.s2b = d.Gcc.s2b;
+  S.fx_s1b = d.Gfx.s1b;
+  S.fx_s2b = d.Gfx.s2b;
+  S.fy_s1b = d.Gfy.s1b;
+  S.fy_s2b = d.Gfy.s2b;
+  S.fz_s1b = d.Gfz.s1b;
+  S.fz_s2b = d.Gfz.s2b;
+  S.px = bc.pW == BBPP_PERIODIC;
+  S.py = bc.pS == BBPP_PERIODIC;
+  S.pz = bc.pB == BBPP_PERIODIC;
+  S.idx = 1. / d.dx;
+  S.idy = 1. / d.dy;
+  S.idz = 1. / d.dz;
+  S.idx2 = 1. / (d.dx * d.dx);
+  S.idy2 = 1. / (d.dy * d.dy);
+  S.idz2 = 1. / (d.dz * d.dz);
+  return S;
+}
+
+int grid_blocks(long long n) {
+  long long b = (n + 255) / 256;
+  return (int)(b < 4096 ? (b > 0 ? b : 1) : 4096);
+}
+
+void check(cudaError_t e, const char *what) {
+  if (e != cudaSuccess) {
+    fprintf(stderr, "N%d >> bbpp pressure solver: %s: %s\n", rank, what, cudaGetErrorString(e));
+    exit(EXIT_FAILURE);
+  }
+}
+
+void solve(bool particles, bool timed) {
+  const char *recname = timed ? "solver_expd_timed.rec" : "solver_expd.rec";
+  struct timeval ts, te;
+  gettimeofday(&ts, 0);
+  ensure_ctx();
+  const bb_dom_struct &d = dom[rank];
+  const Shape S = shape_of(d);
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  const int nb = grid_blocks(n);
+  // rhs into _rhs_p (reference layout), as PP_rhs
+  check(cudaMemset(_rhs_p, 0, sizeof(double) * (size_t)d.Gcc.s3b), "memset rhs");
+  k_rhs_div_b<<<nb, 256>>>(S, rho_f / dt, _u_star, _v_star, _w_star, _rhs_p);
+  check(cudaGetLastError(), "rhs kernel");
+  if (particles) {
+    if (nparts > 0) cuda_part_BC_p();
+    if (!g.mask_valid) {
+      k_mask_from_phase<<<nb, 256>>>(S, _phase, g.mask);
+      check(cudaGetLastError(), "mask kernel");
+      g.mask_valid = true;
+    }
+  }
+  k_refine_pack<<<nb, 256>>>(S, _rhs_p, (particles && nparts > 0) ? g.mask : nullptr, g.b);
+  check(cudaGetLastError(), "refine kernel");
+  check(cudaDeviceSynchronize(), "rhs build");
+
+  bbpp_opts o;
+  bbpp_default_opts(&o);
+  o.precision = BBPP_FP64;
+  o.guess = BBPP_GUESS_ZERO;
+  o.stop = BBPP_STOP_REF_RZ;
+  o.tol = pp_residual;
+  o.max_iter = pp_max_iter;
+  o.replace_every = 50;
+  bbpp_report rep;
+  char rname[256];
+  snprintf(rname, sizeof(rname), "%s", recname);
+  if (timed) {
+    if (stepnum == 1) recorder_PP_init_timed(rname);
+    bbpp_set_profiling(g.ctx, 1);
+  }
+  const int rc = bbpp_solve(g.ctx, particles ? g.mask : nullptr, g.b, g.x, &o, &rep);
+  double t_spmv = 0, t_up = 0;
+  if (timed) {
+    bbpp_kstat ks[16];
+    int nk = 0;
+    bbpp_kernel_stats(g.ctx, ks, 16, &nk);
+    for (int q = 0; q < nk && q < 16; q++) {
+      if (strncmp(ks[q].name, "search_spmv", 11) == 0) t_spmv += ks[q].ms * 1e-3;
+      else t_up += ks[q].ms * 1e-3;
+    }
+    bbpp_set_profiling(g.ctx, 0);
+  }
+  auto record = [&](int niter, double resid, double etime) {
+    if (timed) recorder_PP_timed(rname, niter, resid, etime, t_spmv, 0., 0., t_up, 0., 0., 0., 0.);
+    else recorder_PP(rname, niter, resid, etime);
+  };
+  if (rc == BBPP_TINY_RHS) {
+    gettimeofday(&te, 0);
+    double etime = (te.tv_sec - ts.tv_sec) + (te.tv_usec - ts.tv_usec) * 1.e-6;
+    record(0, 0., etime);
+    if (rank == 0) printf("N%d >> Norm of the rhs is less than %.1e, exiting solver\n", rank, 1.e-8);
+    return;  // phi untouched, as the reference
+  }
+  if (rc == BBPP_NAN) {
+    if (rank == 0) {
+      printf("N%d >> The PP equation did not converge.\n", rank);
+      printf("N%d >> The residual at iteration %d is nan (%lf).\n", rank, rep.iters, sqrt(rep.rz));
+    }
+    exit(EXIT_FAILURE);
+  }
+  if (rc == BBPP_MAX_ITER) {
+    printf("N%d >> The pressure-Poisson equation did not converge.\n", rank);
+    printf("N%d >> (rhs, rhs) is %e\n", rank, rep.bb);
+    printf("N%d >> Residual at iteration %d is %lf\n", rank, rep.iters, sqrt(rep.rz) / sqrt(rep.bb));
+    exit(EXIT_FAILURE);
+  }
+  if (rc != BBPP_CONVERGED) fail("bbpp_solve", rc);
+  k_unpack_phi<<<nb, 256>>>(S, g.x, _phi);
+  check(cudaGetLastError(), "unpack kernel");
+  check(cudaDeviceSynchronize(), "unpack");
+  gettimeofday(&te, 0);
+  double etime = (te.tv_sec - ts.tv_sec) + (te.tv_usec - ts.tv_usec) * 1.e-6;
+  record(rep.iters, sqrt(rep.rz) / sqrt(rep.bb), etime);
+}
+
+}  // namespace
+
+extern "C" void bbpp_bluebottle_release(void) {
+  if (g.ctx) bbpp_destroy(g.ctx);
+  if (g.mask) cudaFree(g.mask);
+  if (g.b) cudaFree(g.b);
+  if (g.x) cudaFree(g.x);
+  g = DropIn();
+}
+
+extern "C" void cuda_PP_init_jacobi_preconditioner(void) {
+  ensure_ctx();
+  const bb_dom_struct &d = dom[rank];
+  const Shape S = shape_of(d);
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  if (NPARTS > 0 && _phase) {
+    k_mask_from_phase<<<grid_blocks(n), 256>>>(S, _phase, g.mask);
+    check(cudaGetLastError(), "mask kernel");
+    g.mask_valid = true;
+  }
+  if (_invM) {
+    int rc = bbpp_invm(g.ctx, _invM);
+    if (rc) fail("bbpp_invm", rc);
+  }
+  check(cudaDeviceSynchronize(), "preconditioner init");
+}
+
+extern "C" void cuda_PP_cg(void) { solve(true, false); }
+
+extern "C" void cuda_PP_cg_noparts(void) { solve(false, false); }
+
+// The reference's timed variant is the particle solve (src/cuda_solver.cu:302-571).
+extern "C" void cuda_PP_cg_timed(void) { solve(true, true); }

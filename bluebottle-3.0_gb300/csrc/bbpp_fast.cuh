@@ -1,0 +1,412 @@
+// bbpp_fast.cuh -- the solver's iteration kernels on the scaled operator.
+//
+// The PCG runs on L = S (-A) with S = 1 / (2/dx^2 + 2/dy^2 + 2/dz^2), so a
+// fluid cell away from walls has diagonal 1 and Jacobi weight 1, and the
+// iteration needs no multiply for them.  With L x = S rhs the iterates are
+// those of the reference's PCG on (-A) x = rhs (alpha and beta are unchanged;
+// (r,z), (r,r) and (rhs,rhs) scale by S, S^2, S^2).  Scaling matters on GB300
+// because FP64 issues at ~1/58 of FP32: these kernels keep FP64 instructions
+// per cell to the stencil's adds, one FMA per update and one per dot.
+//
+// Cells of a solid sphere hold r = p = Ap = x = 0 throughout (their rhs is
+// taken as zero, as part_BC_p makes it, src/particle_kernel.cu:1753): the
+// residual kernel writes r = 0 and x = 0 there, and the search kernel writes
+// Ap = 0 there.  A fluid cell's solid neighbour then contributes p = 0, which
+// is the reference's dropped off-diagonal (src/solver_kernel.cu:691-707).
+//
+//  k1_search  p = invM r + beta p_old on a 32x16 tile plus halo, ring of three
+//             planes in shared memory, loads of plane z+2 in flight while
+//             plane z is computed; Ap = L p and the (p, Ap) partial.
+//  k2_update  x += alpha p, r -= alpha Ap, (r,r) and the wall correction of
+//             (r,z), vector loads.
+//  k_resid_s  r = bscale rhs - L x (solid cells 0) with (r,z), (r,r), (rhs,rhs).
+#pragma once
+
+#include "bbpp_dev.cuh"
+
+namespace bbpp {
+
+constexpr int FX = 32;       // tile width (x): one warp
+constexpr int FY = 16;       // tile height (y): two rows per thread
+constexpr int FHX = FX + 2;  // halo tile width
+constexpr int FHY = FY + 2;
+constexpr int FNT = 256;     // threads
+constexpr int FHE = FHX * FHY;                    // halo elements per plane (612)
+constexpr int FPER = (FHE + FNT - 1) / FNT;       // halo elements per thread (3)
+
+// Scaled-operator constants.  Wall class as in Geo: wx + 3 wy + 9 wz.
+struct GeoL {
+  int nx, ny, nz;
+  int px, py, pz;
+  int iso;             // ax == ay == az
+  long long n;
+  double S;            // scale of L = S (-A)
+  double ax, ay, az;   // S/dx^2, S/dy^2, S/dz^2
+  double dL[27];       // fluid diagonal of L per wall class (dL[0] = 1)
+  double invL[27];     // Jacobi weight 1/dL (invL[0] = 1)
+  float fax, fay, faz;
+  float fdL[27], finvL[27];
+  unsigned long long mx, mxy;  // exact division by nx, nx*ny
+};
+
+template <typename T> __device__ __forceinline__ T gl_ax(const GeoL &G);
+template <> __device__ __forceinline__ double gl_ax<double>(const GeoL &G) { return G.ax; }
+template <> __device__ __forceinline__ float gl_ax<float>(const GeoL &G) { return G.fax; }
+template <typename T> __device__ __forceinline__ T gl_ay(const GeoL &G);
+template <> __device__ __forceinline__ double gl_ay<double>(const GeoL &G) { return G.ay; }
+template <> __device__ __forceinline__ float gl_ay<float>(const GeoL &G) { return G.fay; }
+template <typename T> __device__ __forceinline__ T gl_az(const GeoL &G);
+template <> __device__ __forceinline__ double gl_az<double>(const GeoL &G) { return G.az; }
+template <> __device__ __forceinline__ float gl_az<float>(const GeoL &G) { return G.faz; }
+
+template <typename T>
+__device__ __forceinline__ void load_tabs(const GeoL &G, T *s_dL, T *s_inv) {
+  for (int e = threadIdx.x; e < 27; e += blockDim.x) {
+    if (sizeof(T) == 8) {
+      s_dL[e] = (T)G.dL[e];
+      s_inv[e] = (T)G.invL[e];
+    } else {
+      s_dL[e] = (T)G.fdL[e];
+      s_inv[e] = (T)G.finvL[e];
+    }
+  }
+}
+
+// L p at one cell from its 7 values; cls = wall class; the masked variant has
+// already zeroed the couplings of solid cells.
+template <typename T, bool ISO>
+__device__ __forceinline__ T apply_L(const GeoL &G, const T *s_dL, int cls, T pc, T pe, T pw, T pn, T ps, T pt,
+                                     T pb) {
+  if (ISO) {
+    const T s = ((pe + pw) + (pn + ps)) + (pt + pb);
+    const T na = -gl_ax<T>(G);
+    if (cls == 0) return fma(na, s, pc);
+    return fma(s_dL[cls], pc, na * s);
+  } else {
+    T s = gl_ax<T>(G) * (pe + pw);
+    s = fma(gl_ay<T>(G), pn + ps, s);
+    s = fma(gl_az<T>(G), pt + pb, s);
+    if (cls == 0) return pc - s;
+    return fma(s_dL[cls], pc, -s);
+  }
+}
+
+// ------------------------------------------------------------------ K1 ----
+template <typename T, bool MASK, bool ISO>
+__global__ void __launch_bounds__(FNT) k1_search(const GeoL G, const T *__restrict__ r, const T *__restrict__ pold,
+                                                 T *__restrict__ pnew, T *__restrict__ Ap,
+                                                 const uint8_t *__restrict__ mask, DevState *st, double *partials,
+                                                 int kz) {
+  __shared__ T s_dL[27], s_inv[27];
+  __shared__ T sp[3][FHY][FHX];
+  __shared__ uint8_t sm[3][FHY][FHX + 2];
+  __shared__ double s_red[FNT / 32];
+  if (*(volatile int *)&st->done) return;
+  const bool first = *(volatile int *)&st->first;
+  const T beta = first ? T(0) : (T)(*(volatile double *)&st->beta);
+  load_tabs<T>(G, s_dL, s_inv);
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 31, ty = tid >> 5;  // ty in 0..7; rows ty and ty + 8
+  const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY;
+  const int z0 = blockIdx.z * kz, z1 = min(z0 + kz, G.nz);
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const long long sxy = (long long)nx * ny;
+
+  // halo elements owned by this thread: plane-independent part
+  int e_off[FPER];     // gx + nx*gy, or -1 when there is no cell
+  int e_cls[FPER];     // wall class x + 3y part
+  int e_slot[FPER];    // ly * FHX + lx
+  bool e_own[FPER];    // inside the tile (its p_new is written by this CTA)
+#pragma unroll
+  for (int q = 0; q < FPER; q++) {
+    const int e = tid + q * FNT;
+    e_off[q] = -1;
+    e_cls[q] = 0;
+    e_slot[q] = e;
+    e_own[q] = false;
+    if (e < FHE) {
+      const int ly = e / FHX, lx = e - ly * FHX;
+      const int rx = x0 + lx - 1, ry = y0 + ly - 1;
+      const int gx = halo_index(rx, nx, G.px), gy = halo_index(ry, ny, G.py);
+      if (gx >= 0 && gy >= 0) {
+        e_off[q] = gx + nx * gy;
+        e_cls[q] = wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py);
+        e_own[q] = (rx == gx && ry == gy && lx >= 1 && lx <= FX && ly >= 1 && ly <= FY);
+      }
+    }
+  }
+  __syncthreads();
+
+  T vr[FPER], vp[FPER];
+  uint8_t vm[FPER];
+  int cur_gz = -1;
+  auto issue = [&](int zr) {  // global loads of plane zr into registers
+    const int gz = halo_index(zr, nz, G.pz);
+    cur_gz = gz;
+#pragma unroll
+    for (int q = 0; q < FPER; q++) {
+      vr[q] = T(0);
+      vp[q] = T(0);
+      vm[q] = 0;
+      if (gz >= 0 && e_off[q] >= 0) {
+        const long long c = e_off[q] + sxy * gz;
+        vr[q] = r[c];
+        if (!first) vp[q] = pold[c];
+        if (MASK) vm[q] = mask[c];
+      }
+    }
+  };
+  auto commit = [&](int slot, int zr) {  // p_new from the registers into the ring
+    const int gz = cur_gz;
+    const int wz = (gz >= 0) ? 9 * wall_count(gz, nz, G.pz) : 0;
+    const bool ownz = (zr >= z0 && zr < z1);
+#pragma unroll
+    for (int q = 0; q < FPER; q++) {
+      if (e_slot[q] < FHE) {
+        T val = T(0);
+        if (gz >= 0 && e_off[q] >= 0) {
+          const int cls = e_cls[q] + wz;
+          T z = vr[q];
+          if (cls) z *= s_inv[cls];
+          val = first ? z : fma(beta, vp[q], z);
+          if (ownz && e_own[q]) pnew[e_off[q] + sxy * gz] = val;
+        }
+        (&sp[slot][0][0])[e_slot[q]] = val;
+        (&sm[slot][0][0])[(e_slot[q] / FHX) * (FHX + 2) + e_slot[q] % FHX] = vm[q];
+      }
+    }
+  };
+
+  // prologue: planes z0-1 and z0 in the ring, z0+1 in registers
+  issue(z0 - 1);
+  commit(0, z0 - 1);
+  issue(z0);
+  commit(1, z0);
+  issue(z0 + 1);
+
+  const int gx = x0 + tx;
+  const int gy0 = y0 + ty, gy1 = y0 + ty + 8;
+  const bool m0 = gx < nx && gy0 < ny, m1 = gx < nx && gy1 < ny;
+  const int cxy0 = m0 ? wall_count(gx, nx, G.px) + 3 * wall_count(gy0, ny, G.py) : 0;
+  const int cxy1 = m1 ? wall_count(gx, nx, G.px) + 3 * wall_count(gy1, ny, G.py) : 0;
+  typename Acc<T>::type acc = 0;
+
+  for (int z = z0; z < z1; z++) {
+    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
+    commit(st_, z + 1);             // plane z+1 from registers
+    if (z + 2 <= z1) issue(z + 2);  // loads of plane z+2 fly during this plane's work
+    __syncthreads();
+    const int wz = 9 * wall_count(z, nz, G.pz);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const bool mine = h ? m1 : m0;
+      if (!mine) continue;
+      const int ly = ty + 1 + 8 * h, lx = tx + 1;
+      T pc = sp[sc][ly][lx];
+      T pe = sp[sc][ly][lx + 1], pw = sp[sc][ly][lx - 1];
+      T pn = sp[sc][ly + 1][lx], ps = sp[sc][ly - 1][lx];
+      T pt = sp[st_][ly][lx], pb = sp[sb][ly][lx];
+      const int cls = (h ? cxy1 : cxy0) + wz;
+      T a = apply_L<T, ISO>(G, s_dL, cls, pc, pe, pw, pn, ps, pt, pb);
+      // a solid cell's row is decoupled; a fluid cell's solid neighbour holds
+      // p = 0, so its coupling vanishes without a select
+      if (MASK && sm[sc][ly][lx]) a = T(0);
+      Ap[gx + (long long)nx * (h ? gy1 : gy0) + sxy * z] = a;
+      acc = fma(pc, a, acc);
+    }
+    __syncthreads();
+  }
+  double v[1] = {(double)acc}, tot[1];
+  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
+    st->pAp = tot[0];
+    st->alpha = st->rz / tot[0];
+    st->first = 0;
+  }
+}
+
+// ------------------------------------------------------------------ K2 ----
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { typedef double2 type; };
+template <> struct Vec2<float> { typedef float2 type; };
+
+// Jacobi weight minus one of cell c (0 for interior cells)
+__device__ __forceinline__ int cell_class(const GeoL &G, unsigned int c) {
+  const unsigned int row = fdiv(c, G.mx);
+  const unsigned int k = fdiv(c, G.mxy);
+  const int i = (int)(c - row * (unsigned)G.nx);
+  const int j = (int)(row - k * (unsigned)G.ny);
+  return wall_count(i, G.nx, G.px) + 3 * wall_count(j, G.ny, G.py) + 9 * wall_count((int)k, G.nz, G.pz);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x, T *__restrict__ r,
+                                                 const T *__restrict__ p, const T *__restrict__ Ap, DevState *st,
+                                                 double *partials) {
+  __shared__ T s_dL[27], s_inv[27];
+  __shared__ double s_red[2 * FNT / 32];
+  if (*(volatile int *)&st->done) return;
+  const T alpha = (T)(*(volatile double *)&st->alpha);
+  load_tabs<T>(G, s_dL, s_inv);
+  __syncthreads();
+  const bool walls = !(G.px && G.py && G.pz);
+  typename Acc<T>::type rr = 0, corr = 0;
+  typedef typename Vec2<T>::type V2;
+  const unsigned int n = (unsigned int)G.n;
+  const unsigned int npair = n >> 1;
+  for (unsigned int q = blockIdx.x * FNT + threadIdx.x; q < npair; q += gridDim.x * FNT) {
+    const V2 pv = reinterpret_cast<const V2 *>(p)[q];
+    const V2 av = reinterpret_cast<const V2 *>(Ap)[q];
+    V2 xv = reinterpret_cast<V2 *>(x)[q];
+    V2 rv = reinterpret_cast<V2 *>(r)[q];
+    xv.x = fma(alpha, pv.x, xv.x);
+    xv.y = fma(alpha, pv.y, xv.y);
+    rv.x = fma(-alpha, av.x, rv.x);
+    rv.y = fma(-alpha, av.y, rv.y);
+    reinterpret_cast<V2 *>(x)[q] = xv;
+    reinterpret_cast<V2 *>(r)[q] = rv;
+    rr = fma(rv.x, rv.x, rr);
+    rr = fma(rv.y, rv.y, rr);
+    if (walls) {
+      const int c0 = cell_class(G, 2 * q), c1 = cell_class(G, 2 * q + 1);
+      if (c0) corr = fma((s_inv[c0] - T(1)) * rv.x, rv.x, corr);
+      if (c1) corr = fma((s_inv[c1] - T(1)) * rv.y, rv.y, corr);
+    }
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {  // odd tail
+    const unsigned int c = n - 1;
+    x[c] = fma(alpha, p[c], x[c]);
+    const T rn = fma(-alpha, Ap[c], r[c]);
+    r[c] = rn;
+    rr = fma(rn, rn, rr);
+    const int cl = cell_class(G, c);
+    if (cl) corr = fma((s_inv[cl] - T(1)) * rn, rn, corr);
+  }
+  double v[2] = {(double)rr + (double)corr, (double)rr}, tot[2];
+  if (last_cta_reduce<2>(v, partials, st, gridDim.x, blockIdx.x, s_red, tot) && threadIdx.x == 0)
+    finish_iteration(st, tot[0], tot[1], true);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(FNT) k_axpy2(const GeoL G, T *__restrict__ x, const T *__restrict__ p,
+                                               const DevState *st) {
+  if (*(volatile const int *)&st->done) return;
+  const T alpha = (T)(*(volatile const double *)&st->alpha);
+  const unsigned int n = (unsigned int)G.n;
+  for (unsigned int c = blockIdx.x * FNT + threadIdx.x; c < n; c += gridDim.x * FNT) x[c] = fma(alpha, p[c], x[c]);
+}
+
+// --------------------------------------------------------------- residual --
+// r = bscale rhs - L x on fluid cells, r = 0 (and x = 0 with zero_solid_x) on
+// solid cells.  TXT: type of x and rhs, TR: type of r.  Dots in FP64 of the
+// stored r: (r,z), (r,r); and (rhs,rhs) of the unscaled rhs.
+template <typename TXT, typename TR, bool MASK, bool ISO>
+__global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__ xin, const TXT *__restrict__ rhs,
+                                                 TR *__restrict__ rout, const uint8_t *__restrict__ mask,
+                                                 DevState *st, double *partials, int kz, int mode, double bscale) {
+  __shared__ TXT s_dL[27], s_inv[27];
+  __shared__ TXT sp[3][FHY][FHX];
+  __shared__ uint8_t sm[3][FHY][FHX + 2];
+  __shared__ double s_red[3 * FNT / 32];
+  if (mode == 1 && *(volatile int *)&st->done) return;
+  load_tabs<TXT>(G, s_dL, s_inv);
+  const int tid = threadIdx.x;
+  const int tx = tid & 31, ty = tid >> 5;
+  const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY;
+  const int z0 = blockIdx.z * kz, z1 = min(z0 + kz, G.nz);
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const long long sxy = (long long)nx * ny;
+  __syncthreads();
+  auto load_plane = [&](int slot, int zr) {
+    const int gz = halo_index(zr, nz, G.pz);
+    for (int e = tid; e < FHE; e += FNT) {
+      const int ly = e / FHX, lx = e - ly * FHX;
+      const int gx = halo_index(x0 + lx - 1, nx, G.px), gy = halo_index(y0 + ly - 1, ny, G.py);
+      TXT val = TXT(0);
+      uint8_t m = 0;
+      if (gz >= 0 && gx >= 0 && gy >= 0) {
+        const long long c = gx + (long long)nx * gy + sxy * gz;
+        if (MASK) m = mask[c];
+        val = m ? TXT(0) : xin[c];  // solid cells count as x = 0
+      }
+      sp[slot][ly][lx] = val;
+      sm[slot][ly][lx] = m;
+    }
+  };
+  double rz = 0, rr = 0, bb = 0;
+  load_plane(0, z0 - 1);
+  load_plane(1, z0);
+  const int gx = x0 + tx;
+  for (int z = z0; z < z1; z++) {
+    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
+    load_plane(st_, z + 1);
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int gy = y0 + ty + 8 * h;
+      if (gx >= nx || gy >= ny) continue;
+      const int ly = ty + 1 + 8 * h, lx = tx + 1;
+      const bool mc = MASK && sm[sc][ly][lx] != 0;
+      const long long c = gx + (long long)nx * gy + sxy * z;
+      const TXT bv = rhs[c];
+      bb = fma((double)bv, (double)bv, bb);
+      if (mc) {
+        rout[c] = TR(0);
+        if (mode == 0) xin[c] = TXT(0);
+        continue;
+      }
+      TXT pc = sp[sc][ly][lx];
+      TXT pe = sp[sc][ly][lx + 1], pw = sp[sc][ly][lx - 1];
+      TXT pn = sp[sc][ly + 1][lx], ps = sp[sc][ly - 1][lx];
+      TXT pt = sp[st_][ly][lx], pb = sp[sb][ly][lx];
+      const int cls = wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py) + 9 * wall_count(z, nz, G.pz);
+      const TXT a = apply_L<TXT, ISO>(G, s_dL, cls, pc, pe, pw, pn, ps, pt, pb);
+      const TXT rv = fma((TXT)bscale, bv, -a);
+      const TR ro = (TR)rv;
+      rout[c] = ro;
+      const double rd = (double)rv;
+      rr = fma(rd, rd, rr);
+      rz = fma(rd, (double)s_inv[cls] * rd, rz);
+    }
+    __syncthreads();
+  }
+  double v[3] = {rz, rr, bb}, tot[3];
+  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (last_cta_reduce<3>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
+    const double rz1 = tot[0], rr1 = tot[1];
+    if (mode == 0) {  // init: thresholds from (rhs,rhs) of the unscaled rhs
+      st->bb = tot[2];
+      st->tol2bb = st->tol2bb * tot[2];  // host stores tol^2 * (S or S^2) here
+      st->rz = rz1;
+      st->rz_last = rz1;
+      st->rr = rr1;
+      st->iter = 0;
+      st->first = 1;
+      st->replacements = 0;
+      if (tot[2] < 1e-16) st->done = DONE_TINY;  // src/cuda_solver.cu:178-190
+      else if (st->stop == 1 && rr1 <= st->tol2bb) st->done = DONE_CONVERGED;
+      else st->done = RUNNING;
+    } else if (mode == 1) {
+      st->replacements += 1;
+      finish_iteration(st, rz1, rr1, true);
+    } else {  // confirm
+      st->replacements += 1;
+      st->rz_last = rz1;
+      st->rr = rr1;
+      if (rr1 <= st->tol2bb) {
+        st->done = DONE_CONVERGED;
+      } else if (isnan(rz1)) {
+        st->done = DONE_NAN;
+      } else {
+        st->beta = rz1 / st->rz;
+        st->rz = rz1;
+        st->done = (st->iter > st->max_iter) ? DONE_MAX_ITER : RUNNING;
+      }
+    }
+  }
+}
+
+}  // namespace bbpp

@@ -8,17 +8,19 @@
 
 #include "../../include/bbpp.h"
 #include "bbpp_dev.cuh"
+#include "bbpp_fast.cuh"
 
 struct GraphKey {
   const void *mask = nullptr, *rhs = nullptr, *x = nullptr, *r = nullptr, *p0 = nullptr, *p1 = nullptr,
              *Ap = nullptr, *st = nullptr;
   int len = 0, replace_every = 0, elem = 0;
   bool rr = false;
+  double bscale = 1.0;
   cudaStream_t stream = nullptr;
   bool operator==(const GraphKey &o) const {
     return mask == o.mask && rhs == o.rhs && x == o.x && r == o.r && p0 == o.p0 && p1 == o.p1 && Ap == o.Ap &&
            st == o.st && len == o.len && replace_every == o.replace_every && elem == o.elem && rr == o.rr &&
-           stream == o.stream;
+           bscale == o.bscale && stream == o.stream;
   }
 };
 
@@ -46,10 +48,13 @@ struct NetWork;     // learned-guess workspace (bbpp_net.cu)
 
 struct bbpp_ctx {
   bbpp_grid grid{};
-  bbpp::Geo G{};
+  bbpp::Geo G{};       // unscaled operator (kernel-level entry points, checks)
+  bbpp::GeoL GL{};     // scaled operator of the iteration kernels
   int sms = 1;
-  int kz = 1;          // z planes per stencil CTA
-  dim3 sgrid;          // stencil grid
+  int kz = 1;          // z planes per stencil CTA (unscaled kernels)
+  dim3 sgrid;          // stencil grid (unscaled kernels)
+  int fkz = 1;         // z planes per CTA of the iteration kernels
+  dim3 fgrid;          // grid of the iteration stencil kernels
   int egrid = 1;       // elementwise grid (1-D)
   size_t nparts = 0;   // capacity of partials (per sum)
   cudaStream_t own_stream = nullptr, stream = nullptr;
@@ -86,7 +91,11 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
                   bbpp::DevState *st, bbpp::DevState *hst, int replace_every, bool confirm, bool rr, int *iters_out);
 template <typename T>
 int bbpp_pcg_init(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, bbpp::DevState *st,
-                  bbpp::DevState *hst, double tol, int stop, int max_iter, bool zero_x);
+                  bbpp::DevState *hst, double tol, int stop, int max_iter, bool zero_x, double bscale);
+// r (TR) = bscale rhs - L x (scaled operator), state init mode (0) or confirm (2)
+template <typename TXT, typename TR>
+void bbpp_launch_resid_s(bbpp_ctx *ctx, const uint8_t *mask, TXT *x, const TXT *rhs, TR *r, bbpp::DevState *st,
+                         int mode, double bscale);
 
 // FP32-inner / FP64-refinement method (bbpp_ir.cu)
 int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o, bool zero_x,

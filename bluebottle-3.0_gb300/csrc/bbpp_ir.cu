@@ -12,6 +12,7 @@
 
 #include "bbpp_internal.h"
 #include "bbpp_kernels.cuh"
+#include "bbpp_fast.cuh"
 
 using namespace bbpp;
 
@@ -64,6 +65,7 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
   IrBuffers *b = ctx->ir;
   DevState *st = ctx->st, *hst = ctx->hst;          // outer state
   DevState *sti = ctx->st + 1, *hsti = ctx->hst + 1;  // inner state
+  const double S = ctx->GL.S;
   if (zero_x) CK(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
   int inner_total = 0, outer = 0;
   double bb = 0, rr = 0, rz = 0;
@@ -74,21 +76,15 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
     memset(hst, 0, sizeof(DevState));
     hst->stop = 1;
     CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
-    {
-      const Geo &G = ctx->G;
-      if (mask)
-        k_resid<double, float, true><<<ctx->sgrid, NT, 0, ctx->stream>>>(G, x, rhs, b->r, mask, st, ctx->partials,
-                                                                         ctx->kz, RES_INIT);
-      else
-        k_resid<double, float, false><<<ctx->sgrid, NT, 0, ctx->stream>>>(G, x, rhs, b->r, mask, st, ctx->partials,
-                                                                          ctx->kz, RES_INIT);
-      CK(cudaGetLastError());
-    }
+    // r = S rhs - L x: the inner system L d = r gives the correction in x units
+    bbpp_launch_resid_s<double, float>(ctx, mask, x, rhs, b->r, st, RES_INIT, S);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
     CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     bb = hst->bb;
-    rr = hst->rr;
-    rz = hst->rz;
+    rr = hst->rr / (S * S);  // unscaled (r, r) and (r, z)
+    rz = hst->rz / S;
     if (bb < 1e-16) {
       status = BBPP_TINY_RHS;
       break;
@@ -112,7 +108,7 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
     double itol = o->inner_tol;
     const double need = o->tol / std::sqrt(rel2);
     if (need > itol) itol = std::min(0.5, need * 0.5);
-    int rc = bbpp_pcg_init<float>(ctx, mask, b->r, b->d, b->rd, sti, hsti, itol, 1, o->max_iter, true);
+    int rc = bbpp_pcg_init<float>(ctx, mask, b->r, b->d, b->rd, sti, hsti, itol, 1, o->max_iter, true, 1.0);
     if (rc) return rc;
     float *const p[2] = {b->p[0], b->p[1]};
     int it = 0;

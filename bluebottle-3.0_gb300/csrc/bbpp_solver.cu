@@ -18,6 +18,7 @@
 #include "../../include/bbpp.h"
 #include "bbpp_internal.h"
 #include "bbpp_kernels.cuh"
+#include "bbpp_fast.cuh"
 
 using namespace bbpp;
 
@@ -83,6 +84,35 @@ int bbpp_geo_init(const bbpp_grid *g, Geo *G) {
   G->mx = div_magic((unsigned)g->nx);
   G->mxy = div_magic((unsigned)(g->nx * g->ny));
   return 0;
+}
+
+// Scaled operator L = S (-A), S = 1 / (fluid interior diagonal).
+static void geol_init(const Geo &G, GeoL *L) {
+  memset(L, 0, sizeof(*L));
+  L->nx = G.nx;
+  L->ny = G.ny;
+  L->nz = G.nz;
+  L->px = G.px;
+  L->py = G.py;
+  L->pz = G.pz;
+  L->n = G.n;
+  L->mx = G.mx;
+  L->mxy = G.mxy;
+  const double S = 1.0 / G.tab[0];
+  L->S = S;
+  L->ax = S * G.cx;
+  L->ay = S * G.cy;
+  L->az = S * G.cz;
+  L->iso = (L->ax == L->ay && L->ay == L->az);
+  for (int c = 0; c < 27; c++) {
+    L->dL[c] = (c == 0) ? 1.0 : S * G.tab[c];
+    L->invL[c] = (c == 0) ? 1.0 : (L->dL[c] != 0 ? 1.0 / L->dL[c] : 0.0);
+    L->fdL[c] = (float)L->dL[c];
+    L->finvL[c] = (float)L->invL[c];
+  }
+  L->fax = (float)L->ax;
+  L->fay = (float)L->ay;
+  L->faz = (float)L->az;
 }
 
 namespace bbpp {
@@ -173,6 +203,20 @@ static void stencil_shape(bbpp_ctx *ctx) {
   nzc = (G.nz + kz - 1) / kz;
   ctx->kz = kz;
   ctx->sgrid = dim3(gx, gy, nzc);
+  {
+    const int fx = (G.nx + FX - 1) / FX, fy = (G.ny + FY - 1) / FY;
+    int pf = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k1_search<double, true, true>, FNT, 0);
+    if (pf < 1) pf = 1;
+    const long long tgt = (long long)ctx->sms * pf;
+    int nzf = (int)std::max<long long>(1, tgt / std::max(1, fx * fy));
+    nzf = std::min(nzf, G.nz);
+    int kzf = (G.nz + nzf - 1) / nzf;
+    if (kzf < 8 && G.nz >= 8) kzf = 8;
+    nzf = (G.nz + kzf - 1) / kzf;
+    ctx->fkz = kzf;
+    ctx->fgrid = dim3(fx, fy, nzf);
+  }
   int per_sm2 = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_update<double, true>, NT, 0);
   if (per_sm2 < 1) per_sm2 = 1;
@@ -195,10 +239,13 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
     return rc;
   }
   ctx->grid = *g;
+  geol_init(ctx->G, &ctx->GL);
   ctx->sms = dev_sms();
   stencil_shape(ctx);
   const size_t n = (size_t)ctx->G.n;
-  const size_t nparts = std::max<size_t>((size_t)ctx->sgrid.x * ctx->sgrid.y * ctx->sgrid.z, (size_t)ctx->egrid);
+  const size_t nparts = std::max<size_t>(
+      std::max<size_t>((size_t)ctx->sgrid.x * ctx->sgrid.y * ctx->sgrid.z, (size_t)ctx->egrid),
+      (size_t)ctx->fgrid.x * ctx->fgrid.y * ctx->fgrid.z);
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   ctx->stream = ctx->own_stream;
@@ -309,40 +356,78 @@ static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, c
                                DevState *st) {
   // bytes/cell: read r, p_old (+ mask), write p_new, Ap
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_SEARCH_SPMV : KK_SEARCH_SPMV_F32, 4.0 * sizeof(T) + (mask ? 1 : 0));
-  if (mask)
-    k_search_spmv<T, true><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, r, pold, pnew, Ap, mask, st, ctx->partials,
-                                                               ctx->kz);
-  else
-    k_search_spmv<T, false><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, r, pold, pnew, Ap, mask, st, ctx->partials,
-                                                                ctx->kz);
+  const dim3 g = ctx->fgrid;
+  cudaStream_t s = ctx->stream;
+  if (mask) {
+    if (ctx->GL.iso)
+      k1_search<T, true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, ctx->fkz);
+    else
+      k1_search<T, true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, ctx->fkz);
+  } else {
+    if (ctx->GL.iso)
+      k1_search<T, false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, ctx->fkz);
+    else
+      k1_search<T, false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, ctx->fkz);
+  }
   bbpp_rec_end(ctx);
 }
 
 template <typename T>
 static void launch_update(bbpp_ctx *ctx, T *x, T *r, const T *p, const T *Ap, DevState *st, bool rr) {
+  (void)rr;
   // bytes/cell: read x, r, p, Ap, write x, r
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_UPDATE : KK_UPDATE_F32, 6.0 * sizeof(T));
-  if (rr)
-    k_update<T, true><<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, r, p, Ap, st, ctx->partials);
-  else
-    k_update<T, false><<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, r, p, Ap, st, ctx->partials);
+  k2_update<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, r, p, Ap, st, ctx->partials);
   bbpp_rec_end(ctx);
 }
 
+// general-form residual / SpMV on the unscaled operator (checks, kernel ABI)
 template <typename TXT, typename TR>
 static void launch_resid(bbpp_ctx *ctx, const uint8_t *mask, const TXT *x, const TXT *rhs, TR *r, DevState *st,
                          int mode) {
-  // bytes/cell: read x, rhs (+ mask), write r
-  bbpp_rec_begin(ctx, sizeof(TXT) == 8 ? KK_RESID : KK_RESID_F32,
-                 (rhs ? 2.0 : 1.0) * sizeof(TXT) + sizeof(TR) + (mask ? 1 : 0));
   if (mask)
     k_resid<TXT, TR, true><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, x, rhs, r, mask, st, ctx->partials, ctx->kz,
                                                                mode);
   else
     k_resid<TXT, TR, false><<<ctx->sgrid, NT, 0, ctx->stream>>>(ctx->G, x, rhs, r, mask, st, ctx->partials,
                                                                 ctx->kz, mode);
+}
+
+template <typename TXT, typename TR>
+void bbpp_launch_resid_s(bbpp_ctx *ctx, const uint8_t *mask, TXT *x, const TXT *rhs, TR *r, DevState *st, int mode,
+                         double bscale) {
+  // bytes/cell: read x, rhs (+ mask), write r
+  bbpp_rec_begin(ctx, sizeof(TXT) == 8 ? KK_RESID : KK_RESID_F32, 2.0 * sizeof(TXT) + sizeof(TR) + (mask ? 1 : 0));
+  const dim3 g = ctx->fgrid;
+  cudaStream_t s = ctx->stream;
+  if (mask) {
+    if (ctx->GL.iso)
+      k_resid_s<TXT, TR, true, true><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz, mode,
+                                                       bscale);
+    else
+      k_resid_s<TXT, TR, true, false><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz, mode,
+                                                        bscale);
+  } else {
+    if (ctx->GL.iso)
+      k_resid_s<TXT, TR, false, true><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz, mode,
+                                                        bscale);
+    else
+      k_resid_s<TXT, TR, false, false><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz,
+                                                         mode, bscale);
+  }
   bbpp_rec_end(ctx);
 }
+
+template void bbpp_launch_resid_s<double, double>(bbpp_ctx *, const uint8_t *, double *, const double *, double *,
+                                                  DevState *, int, double);
+template void bbpp_launch_resid_s<double, float>(bbpp_ctx *, const uint8_t *, double *, const double *, float *,
+                                                 DevState *, int, double);
+template void bbpp_launch_resid_s<float, float>(bbpp_ctx *, const uint8_t *, float *, const float *, float *,
+                                                DevState *, int, double);
+
+// bscale of the right-hand side the current solve runs on (S for the user's
+// rhs, 1 for an already scaled one)
+static thread_local double t_bscale = 1.0;
 
 template <typename T>
 static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
@@ -352,9 +437,9 @@ static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T
   launch_search_spmv<T>(ctx, mask, r, pold, pnew, Ap, st);
   if (q % replace_every == 0) {
     bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_AXPY : KK_AXPY_F32, 3.0 * sizeof(T));
-    k_axpy_x<T><<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, pnew, st);
+    k_axpy2<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, pnew, st);
     bbpp_rec_end(ctx);
-    launch_resid<T, T>(ctx, mask, x, rhs, r, st, RES_ITER);
+    bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, RES_ITER, t_bscale);
   } else {
     launch_update<T>(ctx, x, r, pnew, Ap, st, rr);
   }
@@ -378,6 +463,7 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   key.rr = rr;
   key.elem = (int)sizeof(T);
   key.stream = ctx->stream;
+  key.bscale = t_bscale;
   for (auto &gc : ctx->graphs)
     if (gc.key == key) {
       *out = gc.exec;
@@ -484,7 +570,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
         CK(cudaMemcpyAsync(&st->done, &hst->done, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
         break;
       }
-      launch_resid<T, T>(ctx, mask, x, rhs, r, st, RES_CONFIRM);
+      bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, RES_CONFIRM, t_bscale);
       ctx->launches += 1;
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
@@ -503,24 +589,27 @@ template int bbpp_pcg_loop<float>(bbpp_ctx *, const uint8_t *, const float *, fl
 // Initialise a device state and run r = rhs - (-A)x (RES_INIT) for type T.
 template <typename T>
 int bbpp_pcg_init(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, DevState *st, DevState *hst,
-                  double tol, int stop, int max_iter, bool zero_x) {
+                  double tol, int stop, int max_iter, bool zero_x, double bscale) {
   memset(hst, 0, sizeof(DevState));
-  hst->tol2bb = tol * tol;  // multiplied by (rhs,rhs) inside RES_INIT
+  // thresholds on the scaled quantities: (r,z) scales by bscale, (r,r) by
+  // bscale^2; RES_INIT multiplies by the unscaled (rhs,rhs)
+  hst->tol2bb = tol * tol * (stop == 0 ? bscale : bscale * bscale);
+  t_bscale = bscale;
   hst->max_iter = max_iter;
   hst->stop = stop;
   hst->first = 1;
   CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
   if (zero_x) CK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)ctx->G.n, ctx->stream));
-  launch_resid<T, T>(ctx, mask, x, rhs, r, st, RES_INIT);
+  bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, RES_INIT, bscale);
   ctx->launches += 1;
   CK(cudaGetLastError());
   return 0;
 }
 
 template int bbpp_pcg_init<double>(bbpp_ctx *, const uint8_t *, const double *, double *, double *, DevState *,
-                                   DevState *, double, int, int, bool);
+                                   DevState *, double, int, int, bool, double);
 template int bbpp_pcg_init<float>(bbpp_ctx *, const uint8_t *, const float *, float *, float *, DevState *,
-                                  DevState *, double, int, int, bool);
+                                  DevState *, double, int, int, bool, double);
 
 // ------------------------------------------------------------------ solve --
 static int check_opts(const bbpp_opts *o) {
@@ -536,7 +625,8 @@ static int check_opts(const bbpp_opts *o) {
 static int solve_fp64(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o,
                       bool zero_x, bbpp_report *rep) {
   DevState *st = ctx->st, *hst = ctx->hst;
-  int rc = bbpp_pcg_init<double>(ctx, mask, rhs, x, ctx->r, st, hst, o->tol, o->stop, o->max_iter, zero_x);
+  const double S = ctx->GL.S;
+  int rc = bbpp_pcg_init<double>(ctx, mask, rhs, x, ctx->r, st, hst, o->tol, o->stop, o->max_iter, zero_x, S);
   if (rc) return rc;
   double *const p[2] = {ctx->p[0], ctx->p[1]};
   int iters = 0;
@@ -546,8 +636,8 @@ static int solve_fp64(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, dou
   rep->iters = iters;
   rep->replacements = hst->replacements;
   rep->bb = hst->bb;
-  rep->rz = hst->rz_last;
-  rep->rel_resid = hst->bb > 0 ? std::sqrt(std::max(0.0, hst->rr) / hst->bb) : 0.0;
+  rep->rz = hst->rz_last / S;  // back to the unscaled (r, z)
+  rep->rel_resid = hst->bb > 0 ? std::sqrt(std::max(0.0, hst->rr) / hst->bb) / S : 0.0;
   rep->status = status_of(hst->done);
   // algorithmic bytes: per iteration 81 (mask) or 80 B/cell; per replacement
   // x-update 24 + residual 25; init residual 25

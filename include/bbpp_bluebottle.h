@@ -1,0 +1,117 @@
+/*
+ * bbpp_bluebottle.h -- drop-in replacement of the Bluebottle pressure solve.
+ *
+ * libbbpp_bluebottle.so exports the three functions the Bluebottle time loop
+ * calls (src/bluebottle.c:139,228-232,393-395) with the reference's
+ * signatures.  They read the same globals the reference solver reads
+ * (defined by the host program in src/bluebottle.c:438-576 and
+ * src/cuda_bluebottle.cu:34-35) and write the same output (_phi), so a
+ * Bluebottle build links this library in place of src/cuda_solver.cu and
+ * src/solver_kernel.cu.  One rank, one GPU: nprocs must be 1 (the halo
+ * exchange is replaced by on-device periodic wrap).
+ *
+ * The struct layouts below repeat the reference's (src/domain.h:52-94,
+ * 168-210; src/bluebottle.h:662) member for member, because the library
+ * reads the host program's objects of these types.
+ */
+#ifndef BBPP_BLUEBOTTLE_H
+#define BBPP_BLUEBOTTLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef double bb_real; /* the reference's `real` with -DDOUBLE (src/bluebottle.h:45-51) */
+
+/* grid_info, src/domain.h:52-94 */
+typedef struct bb_grid_info {
+  int is, ie, in, isb, ieb, inb;
+  int js, je, jn, jsb, jeb, jnb;
+  int ks, ke, kn, ksb, keb, knb;
+  int _is, _ie, _isb, _ieb;
+  int _js, _je, _jsb, _jeb;
+  int _ks, _ke, _ksb, _keb;
+  int s1, s1b, s2, s2b, s3, s3b;
+  int s2_i, s2_j, s2_k, s2b_i, s2b_j, s2b_k;
+} bb_grid_info;
+
+/* dom_struct, src/domain.h:168-210 */
+typedef struct bb_dom_struct {
+  bb_grid_info Gcc, Gfx, Gfy, Gfz;
+  bb_real xs, xe, xl;
+  int xn;
+  bb_real dx;
+  bb_real ys, ye, yl;
+  int yn;
+  bb_real dy;
+  bb_real zs, ze, zl;
+  int zn;
+  bb_real dz;
+  int rank;
+  int e, w, n, s, t, b;
+  int I, Is, Ie, In;
+  int J, Js, Je, Jn;
+  int K, Ks, Ke, Kn;
+  int S1, S2, S3;
+} bb_dom_struct;
+
+/* The leading members of BC (src/bluebottle.h:662-668); the solver reads
+ * only the pressure boundary types. */
+typedef struct bb_bc_pressure {
+  int pW, pE, pS, pN, pB, pT;
+} bb_bc_pressure;
+
+/* ---- entry points (src/bluebottle.h:3073,3085,3112; defined in the
+ * reference at src/cuda_solver.cu:31,38,573) ---- */
+
+/* Re-derive the solver's view of the particles after the cages were rebuilt:
+ * the one-byte phase mask (solid = _phase > -1) and _invM
+ * (PP_jacobi_init, src/solver_kernel.cu:26-87). */
+void cuda_PP_init_jacobi_preconditioner(void);
+/* Pressure solve with particles (src/cuda_solver.cu:38-300): rhs from
+ * u*,v*,w* (PP_rhs), cuda_part_BC_p(), coeffs_refine, Jacobi PCG from phi = 0
+ * until (r,z) <= pp_residual^2 (rhs,rhs), phi written to _phi's interior,
+ * one row appended through recorder_PP.  NaN residual or more than
+ * pp_max_iter iterations print the reference's messages and exit(EXIT_FAILURE). */
+void cuda_PP_cg(void);
+/* The same without particles (src/cuda_solver.cu:573-761). */
+void cuda_PP_cg_noparts(void);
+/* Per-phase timed variant (src/cuda_solver.cu:302-571): the same solve with
+ * kernel timing on; writes recorder_PP_timed rows to solver_expd_timed.rec.
+ * The search-direction update and both dot products are fused into the two
+ * solver kernels, so spmv holds the fused SpMV kernel, up1 the fused update
+ * kernel (plus residual replacements), and ip1/ar1/ip2/ar2/up2/mpi are 0. */
+void cuda_PP_cg_timed(void);
+
+/* Free the library's private device workspace (no counterpart in the
+ * reference, whose solver uses the host program's buffers). */
+void bbpp_bluebottle_release(void);
+
+/* ---- globals read from the host program ----
+ * Declared for the library's own translation unit only: a Bluebottle source
+ * file includes src/bluebottle.h, which declares the same objects with the
+ * reference's type names and already declares the entry points above. */
+#ifdef BBPP_BLUEBOTTLE_IMPL
+extern bb_dom_struct *dom;
+extern int rank, nprocs;
+extern int NPARTS, nparts;
+extern bb_real rho_f, dt;
+extern bb_real pp_residual;
+extern int pp_max_iter;
+extern int stepnum;
+extern bb_real *_phi, *_rhs_p, *_invM;
+extern bb_real *_u_star, *_v_star, *_w_star;
+extern int *_phase;
+/* ---- functions of the host program the solver calls ---- */
+void cuda_part_BC_p(void);                                              /* src/cuda_particle.cu:1679 */
+void recorder_PP(char *name, int niter, bb_real resid, bb_real etime);  /* src/recorder.c:190 */
+void recorder_PP_init_timed(char *name);                                /* src/recorder.c:223 */
+void recorder_PP_timed(char *name, int niter, bb_real resid, bb_real etime, bb_real etime_spmv,
+                       bb_real etime_ip1, bb_real etime_AR1, bb_real etime_up1, bb_real etime_ip2,
+                       bb_real etime_AR2, bb_real etime_up2, bb_real etime_mpi); /* src/recorder.c:263 */
+#endif /* BBPP_BLUEBOTTLE_IMPL */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

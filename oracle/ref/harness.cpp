@@ -101,7 +101,10 @@ extern "C" void cuda_part_BC_p(void) {
 
 // injected right-hand side: the solver is compiled with PP_rhs renamed to this
 __global__ void PP_rhs_inject(real rho_f_, real *u, real *v, real *w, real *rhs, real dt_) {
-  (void)rho_f_; (void)u; (void)v; (void)w; (void)dt_;
+  if (g_inject.empty()) {  // no injected rhs: run the reference's PP_rhs
+    PP_rhs(rho_f_, u, v, w, rhs, dt_);
+    return;
+  }
   if (threadIdx.x || threadIdx.y || blockIdx.x || blockIdx.y) return;
   const grid_info &G = dom[0].Gcc;
   for (int k = 0; k < G.kn; k++)
@@ -253,6 +256,45 @@ extern "C" int ref_setup(int nx, int ny, int nz, double dx, double dy, double dz
 extern "C" int ref_solve(const double *rhs, double residual, int max_iter, double *phi, int *niter, double *resid) {
   const grid_info &G = dom[0].Gcc;
   g_inject.assign(rhs, rhs + (size_t)G.s3);
+  pp_residual = residual;
+  pp_max_iter = max_iter;
+  g_niter = -1;
+  if (NPARTS > 0) cuda_PP_cg();
+  else cuda_PP_cg_noparts();
+  for (int k = 0; k < G.kn; k++)
+    for (int j = 0; j < G.jn; j++)
+      for (int i = 0; i < G.in; i++) phi[(size_t)i + (size_t)G.in * (j + (size_t)G.jn * k)] = _phi[ccb(i, j, k)];
+  *niter = g_niter;
+  *resid = g_resid;
+  return 0;
+}
+
+static void load_faces(const double *u, const double *v, const double *w) {
+  const dom_struct &d = dom[0];
+  const int nx = d.Gcc.in, ny = d.Gcc.jn, nz = d.Gcc.kn;
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i <= nx; i++)
+        _u_star[GFX_LOC(i + 1, j + 1, k + 1, d.Gfx.s1b, d.Gfx.s2b)] = u[i + (size_t)(nx + 1) * (j + (size_t)ny * k)];
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j <= ny; j++)
+      for (int i = 0; i < nx; i++)
+        _v_star[GFY_LOC(i + 1, j + 1, k + 1, d.Gfy.s1b, d.Gfy.s2b)] = v[i + (size_t)nx * (j + (size_t)(ny + 1) * k)];
+  for (int k = 0; k <= nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++)
+        _w_star[GFZ_LOC(i + 1, j + 1, k + 1, d.Gfz.s1b, d.Gfz.s2b)] = w[i + (size_t)nx * (j + (size_t)ny * k)];
+}
+
+// The whole reference solve including its rhs build from u*, v*, w*
+// (dense face arrays as ref_rhs), as the time loop calls it.
+extern "C" int ref_solve_u(double rho, double dtt, const double *u, const double *v, const double *w,
+                           double residual, int max_iter, double *phi, int *niter, double *resid) {
+  const grid_info &G = dom[0].Gcc;
+  load_faces(u, v, w);
+  g_inject.clear();
+  rho_f = rho;
+  dt = dtt;
   pp_residual = residual;
   pp_max_iter = max_iter;
   g_niter = -1;

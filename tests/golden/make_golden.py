@@ -37,6 +37,7 @@ def load():
     L.ref_spmv.argtypes = [v, v]
     L.ref_invm.argtypes = [v]
     L.ref_rhs.argtypes = [ctypes.c_double, ctypes.c_double, v, v, v, v]
+    L.ref_solve_u.argtypes = [ctypes.c_double, ctypes.c_double, v, v, v, ctypes.c_double, ctypes.c_int, v, v, v]
     return L
 
 
@@ -130,6 +131,40 @@ def main():
                             niter=it.value, resid=rs.value)
         manifest[name] = {"kind": "solve", "dims": dims, "bc": bc, "pp_residual": resid, "niter": it.value,
                           "resid": rs.value, "solid_cells": int(mask.sum()) if mask is not None else 0}
+        print(name, it.value, rs.value)
+    # whole solves as the time loop calls them: rhs from u*, v*, w* (PP_rhs),
+    # particle masking, coeffs_refine, PCG (cuda_PP_cg / cuda_PP_cg_noparts)
+    dropin_cases = [
+        ("dropin_ppn_spheres_20", (20, 18, 16), (P, P, P, P, N, N), 5, 1e-9),
+        ("dropin_ppn_noparts_16", (16, 16, 12), (P, P, P, P, N, N), 0, 1e-10),
+    ]
+    for name, dims, bc, nsph, resid in dropin_cases:
+        nx, ny, nz = dims
+        h = (1 / nx, 1 / ny, 1 / nz)
+        mask = None
+        if nsph:
+            cents = rng.random((nsph, 3))
+            cents[:, 2] = 0.25 + 0.5 * cents[:, 2]
+            mask = spheres_mask(dims, h, bc, cents, np.full(nsph, 0.15))
+        u = rng.normal(size=(nz, ny, nx + 1))
+        v = rng.normal(size=(nz, ny + 1, nx))
+        w = rng.normal(size=(nz + 1, ny, nx))
+        # periodic x, y: the face on the far side equals the first face;
+        # Neumann z: no flow through the walls (a consistent rhs without spheres)
+        u[:, :, nx] = u[:, :, 0]
+        v[:, ny, :] = v[:, 0, :]
+        w[0] = 0.0
+        w[nz] = 0.0
+        setup(L, dims, h, bc, mask)
+        phi = np.zeros((nz, ny, nx))
+        it, rs = ctypes.c_int(), ctypes.c_double()
+        L.ref_solve_u(1.3, 0.01, u.ctypes.data, v.ctypes.data, w.ctypes.data, resid, 20000, phi.ctypes.data,
+                      ctypes.byref(it), ctypes.byref(rs))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), dims=dims, h=h, bc=bc, u=u, v=v, w=w, rho_f=1.3,
+                            dt=0.01, mask=mask if mask is not None else np.zeros(0, np.uint8), pp_residual=resid,
+                            phi=phi, niter=it.value, resid=rs.value)
+        manifest[name] = {"kind": "dropin", "dims": dims, "bc": bc, "pp_residual": resid, "niter": it.value,
+                          "resid": rs.value}
         print(name, it.value, rs.value)
     json.dump(manifest, open(os.path.join(HERE, "manifest.json"), "w"), indent=1)
 
