@@ -216,6 +216,9 @@ void solve(bool particles, bool timed) {
   check(cudaMemset(_rhs_p, 0, sizeof(double) * (size_t)d.Gcc.s3b), "memset rhs");
   k_rhs_div_b<<<nb, 256>>>(S, rho_f / dt, _u_star, _v_star, _w_star, _rhs_p);
   check(cudaGetLastError(), "rhs kernel");
+  // the particle solve needs the phase field; without one it is the
+  // particle-free operator
+  particles = particles && NPARTS > 0 && _phase != nullptr;
   if (particles) {
     if (nparts > 0) cuda_part_BC_p();
     if (!g.mask_valid) {

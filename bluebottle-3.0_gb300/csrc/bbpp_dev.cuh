@@ -40,6 +40,7 @@ struct DevState {
   int replacements;
   unsigned int ticket;  // arrival counter of the last-CTA reductions
   int pad;
+  double tiny;     // (rhs,rhs) below this ends the solve at once (DONE_TINY)
 };
 
 // Geometry and per-wall-class constants.  A cell's wall class is

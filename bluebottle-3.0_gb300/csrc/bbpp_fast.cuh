@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       st->iter = 0;
       st->first = 1;
       st->replacements = 0;
-      if (tot[2] < 1e-16) st->done = DONE_TINY;  // src/cuda_solver.cu:178-190
+      if (tot[2] < st->tiny) st->done = DONE_TINY;  // src/cuda_solver.cu:178-190
       else if (st->stop == 1 && rr1 <= st->tol2bb) st->done = DONE_CONVERGED;
       else st->done = RUNNING;
     } else if (mode == 1) {

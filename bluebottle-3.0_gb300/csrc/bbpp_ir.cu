@@ -75,6 +75,7 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
     // outer residual in FP64, rounded to FP32 for the inner right-hand side
     memset(hst, 0, sizeof(DevState));
     hst->stop = 1;
+    hst->tiny = 1e-16;
     CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
     // r = S rhs - L x: the inner system L d = r gives the correction in x units
     bbpp_launch_resid_s<double, float>(ctx, mask, x, rhs, b->r, st, RES_INIT, S);

@@ -594,6 +594,9 @@ int bbpp_pcg_init(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
   // thresholds on the scaled quantities: (r,z) scales by bscale, (r,r) by
   // bscale^2; RES_INIT multiplies by the unscaled (rhs,rhs)
   hst->tol2bb = tol * tol * (stop == 0 ? bscale : bscale * bscale);
+  // the reference's absolute exit (rhs,rhs) < 1e-16 applies to a user's
+  // right-hand side; an inner correction system only stops on an exact zero
+  hst->tiny = (bscale == 1.0) ? 2.2250738585072014e-308 : 1e-16;
   t_bscale = bscale;
   hst->max_iter = max_iter;
   hst->stop = stop;

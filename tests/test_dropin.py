@@ -280,7 +280,7 @@ def test_dropin_max_iter_exits_like_reference(bbpp_lib):
         H.lib.cuda_PP_cg()
         print("returned")
     """) % ([os.path.join(ROOT, "tests"), os.path.join(ROOT, "bluebottle-3.0_gb300"), os.path.join(ROOT, "oracle")],
-           DROPIN[0])
+           [n for n in DROPIN if "spheres" in n][0])
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
     assert r.returncode == 1, r.stdout + r.stderr
     assert "did not converge" in r.stdout and "returned" not in r.stdout
