@@ -126,6 +126,21 @@ int bbpp_invm(bbpp_ctx *ctx, double *invM);
 int bbpp_residual(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x,
                   double *r, double *rr, double *bb);
 
+/* The residual of bbpp_residual without a context and without allocating:
+ * for callers that cannot allocate device memory while they run (all buffers
+ * sized at start-up, a fixed device-memory budget, or a loop that must not
+ * call the allocator).  No counterpart in the reference.  Reduction scratch
+ * is a static device array holding one state and BBPP_NOALLOC_MAX_CTAS x 3
+ * partial sums (~200 KB per GPU, kept until exit); grids needing more than
+ * BBPP_NOALLOC_MAX_CTAS column tiles of 32x8 cells are rejected
+ * (BBPP_BAD_ARG).  Calls share that scratch: calls overlapping on the GPU
+ * race.  The first call on a device looks up the scratch address and should
+ * come before any stream capture.  mask/rhs/x/r are device pointers; stream
+ * is a cudaStream_t or NULL.  rr, bb receive (r,r) and (rhs,rhs). */
+#define BBPP_NOALLOC_MAX_CTAS 8192
+int bbpp_residual_noalloc(const bbpp_grid *g, const uint8_t *mask, const double *rhs,
+                          const double *x, double *r, double *rr, double *bb, void *stream);
+
 /* Phase mask of spheres, on the device (src/particle_kernel.cu:148-253):
  * cell (i,j,k) is solid when floor(d/r) < 1, d the distance of its centre
  * ((i+0.5)dx + xs, ...) from a sphere centre; periodic directions also test
