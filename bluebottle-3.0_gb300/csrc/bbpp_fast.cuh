@@ -77,6 +77,7 @@ __device__ __forceinline__ void load_tabs(const GeoL &G, T *s_dL, T *s_inv) {
 template <typename T, bool ISO>
 __device__ __forceinline__ T apply_L(const GeoL &G, const T *s_dL, int cls, T pc, T pe, T pw, T pn, T ps, T pt,
                                      T pb) {
+  // cls is a literal 0 on the interior path, so only one form is emitted there
   if (ISO) {
     const T s = ((pe + pw) + (pn + ps)) + (pt + pb);
     const T na = -gl_ax<T>(G);
@@ -157,23 +158,41 @@ __global__ void __launch_bounds__(FNT) k1_search(const GeoL G, const T *__restri
       }
     }
   };
+  // Walls only in z (periodic x and y): a plane's cells share one wall class,
+  // so interior planes take a path without any per-cell class arithmetic.
+  // (A per-cell branch would be if-converted into predicated FP64
+  // instructions, which still occupy the FP64 pipe.)
+  const bool xy_walls = !(G.px && G.py);
   auto commit = [&](int slot, int zr) {  // p_new from the registers into the ring
     const int gz = cur_gz;
     const int wz = (gz >= 0) ? 9 * wall_count(gz, nz, G.pz) : 0;
     const bool ownz = (zr >= z0 && zr < z1);
+    if (!xy_walls && wz == 0) {  // interior plane: Jacobi weight 1
 #pragma unroll
-    for (int q = 0; q < FPER; q++) {
-      if (e_slot[q] < FHE) {
-        T val = T(0);
-        if (gz >= 0 && e_off[q] >= 0) {
-          const int cls = e_cls[q] + wz;
-          T z = vr[q];
-          if (cls) z *= s_inv[cls];
-          val = first ? z : fma(beta, vp[q], z);
-          if (ownz && e_own[q]) pnew[e_off[q] + sxy * gz] = val;
+      for (int q = 0; q < FPER; q++) {
+        if (e_slot[q] < FHE) {
+          T val = T(0);
+          if (gz >= 0 && e_off[q] >= 0) {
+            val = first ? vr[q] : fma(beta, vp[q], vr[q]);
+            if (ownz && e_own[q]) pnew[e_off[q] + sxy * gz] = val;
+          }
+          (&sp[slot][0][0])[e_slot[q]] = val;
+          (&sm[slot][0][0])[(e_slot[q] / FHX) * (FHX + 2) + e_slot[q] % FHX] = vm[q];
         }
-        (&sp[slot][0][0])[e_slot[q]] = val;
-        (&sm[slot][0][0])[(e_slot[q] / FHX) * (FHX + 2) + e_slot[q] % FHX] = vm[q];
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < FPER; q++) {
+        if (e_slot[q] < FHE) {
+          T val = T(0);
+          if (gz >= 0 && e_off[q] >= 0) {
+            const T z = vr[q] * s_inv[e_cls[q] + wz];
+            val = first ? z : fma(beta, vp[q], z);
+            if (ownz && e_own[q]) pnew[e_off[q] + sxy * gz] = val;
+          }
+          (&sp[slot][0][0])[e_slot[q]] = val;
+          (&sm[slot][0][0])[(e_slot[q] / FHX) * (FHX + 2) + e_slot[q] % FHX] = vm[q];
+        }
       }
     }
   };
@@ -198,22 +217,303 @@ __global__ void __launch_bounds__(FNT) k1_search(const GeoL G, const T *__restri
     if (z + 2 <= z1) issue(z + 2);  // loads of plane z+2 fly during this plane's work
     __syncthreads();
     const int wz = 9 * wall_count(z, nz, G.pz);
+    if (!xy_walls && wz == 0) {
+      // interior plane: diagonal 1, no wall arithmetic
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        if (!(h ? m1 : m0)) continue;
+        const int ly = ty + 1 + 8 * h, lx = tx + 1;
+        const T pc = sp[sc][ly][lx];
+        T a = apply_L<T, ISO>(G, s_dL, 0, pc, sp[sc][ly][lx + 1], sp[sc][ly][lx - 1], sp[sc][ly + 1][lx],
+                              sp[sc][ly - 1][lx], sp[st_][ly][lx], sp[sb][ly][lx]);
+        // a solid cell's row is decoupled; a fluid cell's solid neighbour holds
+        // p = 0, so its coupling vanishes without a select
+        if (MASK && sm[sc][ly][lx]) a = T(0);
+        Ap[gx + (long long)nx * (h ? gy1 : gy0) + sxy * z] = a;
+        acc = fma(pc, a, acc);
+      }
+    } else {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        if (!(h ? m1 : m0)) continue;
+        const int ly = ty + 1 + 8 * h, lx = tx + 1;
+        const T pc = sp[sc][ly][lx];
+        const int cls = (h ? cxy1 : cxy0) + wz;
+        T a = apply_L<T, ISO>(G, s_dL, cls, pc, sp[sc][ly][lx + 1], sp[sc][ly][lx - 1], sp[sc][ly + 1][lx],
+                              sp[sc][ly - 1][lx], sp[st_][ly][lx], sp[sb][ly][lx]);
+        if (MASK && sm[sc][ly][lx]) a = T(0);
+        Ap[gx + (long long)nx * (h ? gy1 : gy0) + sxy * z] = a;
+        acc = fma(pc, a, acc);
+      }
+    }
+    __syncthreads();
+  }
+  double v[1] = {(double)acc}, tot[1];
+  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
+    st->pAp = tot[0];
+    st->alpha = st->rz / tot[0];
+    st->first = 0;
+  }
+}
+
+// ------------------------------------------------------------ K1, pairs ---
+// The same search kernel with two x-adjacent cells per thread: a tile is 64 x
+// 16 cells (32 x 8 threads, two rows each).  Halo rows are loaded as aligned
+// pairs into shared rows padded so the pairs stay aligned (index 0 pad, 1 west
+// halo, 2..65 tile, 66 east halo); the two edge columns are scalar loads.
+// Only the thread's own cells need the mask (Ap = 0 in a solid cell), so it
+// is read straight from global memory.  Pairs need an even nx; odd nx uses
+// scalar loads.
+constexpr int PX = 64;          // tile width
+constexpr int PY = 16;          // tile height
+constexpr int PW = PX + 4;      // padded shared row
+constexpr int PHY = PY + 2;     // rows with halo
+constexpr int PROWS = (PHY + 7) / 8;  // halo rows per thread (3)
+
+template <typename T> struct V2of;
+template <> struct V2of<double> { typedef double2 type; };
+template <> struct V2of<float> { typedef float2 type; };
+
+template <typename T, bool MASK, bool ISO>
+__global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const GeoL G, const T *__restrict__ r, const T *__restrict__ pold,
+                                                  T *__restrict__ pnew, T *__restrict__ Ap,
+                                                  const uint8_t *__restrict__ mask, DevState *st, double *partials,
+                                                  int kz) {
+  typedef typename V2of<T>::type V2;
+  __shared__ T s_dL[27], s_inv[27];
+  __shared__ __align__(16) T sp[3][PHY][PW];
+  __shared__ double s_red[FNT / 32];
+  if (*(volatile int *)&st->done) return;
+  const bool first = *(volatile int *)&st->first;
+  const T beta = first ? T(0) : (T)(*(volatile double *)&st->beta);
+  load_tabs<T>(G, s_dL, s_inv);
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 31, ty = tid >> 5;
+  const int x0 = blockIdx.x * PX, y0 = blockIdx.y * PY;
+  const int z0 = blockIdx.z * kz, z1 = min(z0 + kz, G.nz);
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const unsigned int plane = (unsigned int)nx * (unsigned int)ny;
+  const bool vec = !(nx & 1);
+  const bool xy_walls = !(G.px && G.py);
+
+  // pair loads: rows ly = ty + 8k, columns x0 + 2tx, +1
+  const int gxp = x0 + 2 * tx;
+  const int npair = (gxp + 1 < nx) ? 2 : (gxp < nx ? 1 : 0);  // own cells of the pair
+  // halo cells of the pair slot: in a partial tile the slot just past the
+  // grid holds the periodic image (cell 0) of the east neighbour
+  const int gxa = halo_index(gxp, nx, G.px), gxb = halo_index(gxp + 1, nx, G.px);
+  const bool pair_full = vec && gxp + 1 < nx;
+  const int wxp0 = gxa >= 0 ? wall_count(gxa, nx, G.px) : 0;
+  const int wxp1 = gxb >= 0 ? wall_count(gxb, nx, G.px) : 0;
+  int row_off[PROWS];  // nx * gy of the row, or -1
+  int row_wy[PROWS];
+#pragma unroll
+  for (int k = 0; k < PROWS; k++) {
+    const int ly = ty + 8 * k;
+    row_off[k] = -1;
+    row_wy[k] = 0;
+    if (ly < PHY) {
+      const int gy = halo_index(y0 + ly - 1, ny, G.py);
+      if (gy >= 0) {
+        row_off[k] = nx * gy;
+        row_wy[k] = 3 * wall_count(gy, ny, G.py);
+      }
+    }
+  }
+  // edge column element: tid < 2*PHY -> side = tid / PHY, row = tid % PHY
+  int edge_off = -1, edge_cls = 0, edge_ly = 0, edge_col = 0;
+  if (tid < 2 * PHY) {
+    const int side = tid / PHY;
+    edge_ly = tid - side * PHY;
+    edge_col = side ? PX + 2 : 1;
+    const int gx = halo_index(side ? x0 + PX : x0 - 1, nx, G.px);
+    const int gy = halo_index(y0 + edge_ly - 1, ny, G.py);
+    if (gx >= 0 && gy >= 0) {
+      edge_off = gx + nx * gy;
+      edge_cls = wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py);
+    }
+  }
+  __syncthreads();
+
+  T vr[PROWS][2], vp[PROWS][2], er = T(0), ep = T(0);
+  int cur_gz = -1;
+  auto issue = [&](int zr) {
+    const int gz = halo_index(zr, nz, G.pz);
+    cur_gz = gz;
+    const unsigned int zoff = gz >= 0 ? plane * (unsigned int)gz : 0u;
+#pragma unroll
+    for (int k = 0; k < PROWS; k++) {
+      vr[k][0] = vr[k][1] = vp[k][0] = vp[k][1] = T(0);
+      if (gz >= 0 && row_off[k] >= 0) {
+        const unsigned int rowz = zoff + (unsigned int)row_off[k];
+        if (pair_full) {
+          const unsigned int c = rowz + (unsigned int)gxp;
+          const V2 a = *reinterpret_cast<const V2 *>(r + c);
+          vr[k][0] = a.x;
+          vr[k][1] = a.y;
+          if (!first) {
+            const V2 b = *reinterpret_cast<const V2 *>(pold + c);
+            vp[k][0] = b.x;
+            vp[k][1] = b.y;
+          }
+        } else {
+          if (gxa >= 0) {
+            vr[k][0] = r[rowz + gxa];
+            if (!first) vp[k][0] = pold[rowz + gxa];
+          }
+          if (gxb >= 0) {
+            vr[k][1] = r[rowz + gxb];
+            if (!first) vp[k][1] = pold[rowz + gxb];
+          }
+        }
+      }
+    }
+    er = ep = T(0);
+    if (gz >= 0 && edge_off >= 0) {
+      const unsigned int c = zoff + (unsigned int)edge_off;
+      er = r[c];
+      if (!first) ep = pold[c];
+    }
+  };
+  auto commit = [&](int slot, int zr) {
+    const int gz = cur_gz;
+    const int wz = (gz >= 0) ? 9 * wall_count(gz, nz, G.pz) : 0;
+    const bool ownz = (zr >= z0 && zr < z1) && gz >= 0;
+    const unsigned int zoff = gz >= 0 ? plane * (unsigned int)gz : 0u;
+    if (!xy_walls && wz == 0) {  // interior plane, periodic x/y: Jacobi weight 1
+#pragma unroll
+      for (int k = 0; k < PROWS; k++) {
+        const int ly = ty + 8 * k;
+        if (ly >= PHY) continue;
+        V2 v;  // slots without a cell hold r = p_old = 0, so they stay 0
+        v.x = first ? vr[k][0] : fma(beta, vp[k][0], vr[k][0]);
+        v.y = first ? vr[k][1] : fma(beta, vp[k][1], vr[k][1]);
+        *reinterpret_cast<V2 *>(&sp[slot][ly][2 + 2 * tx]) = v;
+        if (ownz && ly >= 1 && ly <= PY && row_off[k] >= 0 && y0 + ly - 1 < ny && npair > 0) {
+          const unsigned int c = zoff + (unsigned int)row_off[k] + (unsigned int)gxp;
+          if (pair_full) {
+            *reinterpret_cast<V2 *>(pnew + c) = v;
+          } else {
+            pnew[c] = v.x;
+            if (npair == 2) pnew[c + 1] = v.y;
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < PROWS; k++) {
+        const int ly = ty + 8 * k;
+        if (ly >= PHY) continue;
+        V2 v;
+        v.x = v.y = T(0);
+        if (gz >= 0 && row_off[k] >= 0) {
+          const T z0v = vr[k][0] * s_inv[wxp0 + row_wy[k] + wz];
+          const T z1v = vr[k][1] * s_inv[wxp1 + row_wy[k] + wz];
+          v.x = first ? z0v : fma(beta, vp[k][0], z0v);
+          v.y = first ? z1v : fma(beta, vp[k][1], z1v);
+        }
+        *reinterpret_cast<V2 *>(&sp[slot][ly][2 + 2 * tx]) = v;
+        if (ownz && ly >= 1 && ly <= PY && row_off[k] >= 0 && y0 + ly - 1 < ny && npair > 0) {
+          const unsigned int c = zoff + (unsigned int)row_off[k] + (unsigned int)gxp;
+          if (pair_full) {
+            *reinterpret_cast<V2 *>(pnew + c) = v;
+          } else {
+            pnew[c] = v.x;
+            if (npair == 2) pnew[c + 1] = v.y;
+          }
+        }
+      }
+    }
+    if (tid < 2 * PHY) {
+      T v = T(0);
+      if (gz >= 0 && edge_off >= 0) {
+        const int cls = edge_cls + wz;
+        const T z = cls ? er * s_inv[cls] : er;
+        v = first ? z : fma(beta, ep, z);
+      }
+      sp[slot][edge_ly][edge_col] = v;
+    }
+  };
+
+  issue(z0 - 1);
+  commit(0, z0 - 1);
+  issue(z0);
+  commit(1, z0);
+  issue(z0 + 1);
+
+  const int gy0 = y0 + ty, gy1 = y0 + ty + 8;
+  const bool m0 = npair > 0 && gy0 < ny, m1 = npair > 0 && gy1 < ny;
+  const int cy0 = m0 ? 3 * wall_count(gy0, ny, G.py) : 0;
+  const int cy1 = m1 ? 3 * wall_count(gy1, ny, G.py) : 0;
+  typename Acc<T>::type acc = 0;
+
+  for (int z = z0; z < z1; z++) {
+    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
+    commit(st_, z + 1);
+    if (z + 2 <= z1) issue(z + 2);
+    // own-cell mask of this plane (used after the barrier)
+    uint8_t mk[2][2] = {{0, 0}, {0, 0}};
+    if (MASK) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        if (!(h ? m1 : m0)) continue;
+        const unsigned int c = plane * (unsigned int)z + (unsigned int)nx * (unsigned int)(h ? gy1 : gy0) + gxp;
+        if (pair_full) {
+          const uchar2 mm = *reinterpret_cast<const uchar2 *>(mask + c);
+          mk[h][0] = mm.x;
+          mk[h][1] = mm.y;
+        } else {
+          mk[h][0] = mask[c];
+          if (npair == 2) mk[h][1] = mask[c + 1];
+        }
+      }
+    }
+    __syncthreads();
+    const int wz = 9 * wall_count(z, nz, G.pz);
+    const bool interior = !xy_walls && wz == 0;
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-      const bool mine = h ? m1 : m0;
-      if (!mine) continue;
-      const int ly = ty + 1 + 8 * h, lx = tx + 1;
-      T pc = sp[sc][ly][lx];
-      T pe = sp[sc][ly][lx + 1], pw = sp[sc][ly][lx - 1];
-      T pn = sp[sc][ly + 1][lx], ps = sp[sc][ly - 1][lx];
-      T pt = sp[st_][ly][lx], pb = sp[sb][ly][lx];
-      const int cls = (h ? cxy1 : cxy0) + wz;
-      T a = apply_L<T, ISO>(G, s_dL, cls, pc, pe, pw, pn, ps, pt, pb);
-      // a solid cell's row is decoupled; a fluid cell's solid neighbour holds
-      // p = 0, so its coupling vanishes without a select
-      if (MASK && sm[sc][ly][lx]) a = T(0);
-      Ap[gx + (long long)nx * (h ? gy1 : gy0) + sxy * z] = a;
-      acc = fma(pc, a, acc);
+      if (!(h ? m1 : m0)) continue;
+      const int ly = ty + 1 + 8 * h;
+      const int col = 2 + 2 * tx;
+      const V2 c = *reinterpret_cast<const V2 *>(&sp[sc][ly][col]);
+      const V2 n = *reinterpret_cast<const V2 *>(&sp[sc][ly + 1][col]);
+      const V2 s = *reinterpret_cast<const V2 *>(&sp[sc][ly - 1][col]);
+      const V2 t = *reinterpret_cast<const V2 *>(&sp[st_][ly][col]);
+      const V2 b = *reinterpret_cast<const V2 *>(&sp[sb][ly][col]);
+      const T w = sp[sc][ly][col - 1], e = sp[sc][ly][col + 2];
+      T a0, a1;
+      if (interior) {
+        a0 = apply_L<T, ISO>(G, s_dL, 0, c.x, c.y, w, n.x, s.x, t.x, b.x);
+        a1 = apply_L<T, ISO>(G, s_dL, 0, c.y, e, c.x, n.y, s.y, t.y, b.y);
+      } else {
+        const int cy = (h ? cy1 : cy0) + wz;
+        a0 = apply_L<T, ISO>(G, s_dL, wxp0 + cy, c.x, c.y, w, n.x, s.x, t.x, b.x);
+        a1 = apply_L<T, ISO>(G, s_dL, wxp1 + cy, c.y, e, c.x, n.y, s.y, t.y, b.y);
+      }
+      if (MASK) {
+        if (mk[h][0]) a0 = T(0);
+        if (mk[h][1]) a1 = T(0);
+      }
+      const unsigned int cc = plane * (unsigned int)z + (unsigned int)nx * (unsigned int)(h ? gy1 : gy0) + gxp;
+      if (pair_full) {
+        V2 o;
+        o.x = a0;
+        o.y = a1;
+        *reinterpret_cast<V2 *>(Ap + cc) = o;
+        acc = fma(c.x, a0, acc);
+        acc = fma(c.y, a1, acc);
+      } else {
+        Ap[cc] = a0;
+        acc = fma(c.x, a0, acc);
+        if (npair == 2) {
+          Ap[cc + 1] = a1;
+          acc = fma(c.y, a1, acc);
+        }
+      }
     }
     __syncthreads();
   }
@@ -241,6 +541,26 @@ __device__ __forceinline__ int cell_class(const GeoL &G, unsigned int c) {
   return wall_count(i, G.nx, G.px) + 3 * wall_count(j, G.ny, G.py) + 9 * wall_count((int)k, G.nz, G.pz);
 }
 
+// One pair of cells: x += alpha p, r -= alpha Ap; returns the new r.
+template <typename T, typename V2>
+__device__ __forceinline__ V2 update_pair(unsigned int q, T alpha, T *__restrict__ x, T *__restrict__ r,
+                                          const T *__restrict__ p, const T *__restrict__ Ap) {
+  const V2 pv = reinterpret_cast<const V2 *>(p)[q];
+  const V2 av = reinterpret_cast<const V2 *>(Ap)[q];
+  V2 xv = reinterpret_cast<V2 *>(x)[q];
+  V2 rv = reinterpret_cast<V2 *>(r)[q];
+  xv.x = fma(alpha, pv.x, xv.x);
+  xv.y = fma(alpha, pv.y, xv.y);
+  rv.x = fma(-alpha, av.x, rv.x);
+  rv.y = fma(-alpha, av.y, rv.y);
+  reinterpret_cast<V2 *>(x)[q] = xv;
+  reinterpret_cast<V2 *>(r)[q] = rv;
+  return rv;
+}
+
+// (r,z) = (r,r) + sum over wall cells of (invL - 1) r^2.  Cells of interior
+// planes carry no class arithmetic: with periodic x and y the pairs of the two
+// z-wall planes run in loops of their own with one weight each.
 template <typename T>
 __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x, T *__restrict__ r,
                                                  const T *__restrict__ p, const T *__restrict__ Ap, DevState *st,
@@ -251,38 +571,49 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x
   const T alpha = (T)(*(volatile double *)&st->alpha);
   load_tabs<T>(G, s_dL, s_inv);
   __syncthreads();
-  const bool walls = !(G.px && G.py && G.pz);
   typename Acc<T>::type rr = 0, corr = 0;
   typedef typename Vec2<T>::type V2;
   const unsigned int n = (unsigned int)G.n;
-  const unsigned int npair = n >> 1;
-  for (unsigned int q = blockIdx.x * FNT + threadIdx.x; q < npair; q += gridDim.x * FNT) {
-    const V2 pv = reinterpret_cast<const V2 *>(p)[q];
-    const V2 av = reinterpret_cast<const V2 *>(Ap)[q];
-    V2 xv = reinterpret_cast<V2 *>(x)[q];
-    V2 rv = reinterpret_cast<V2 *>(r)[q];
-    xv.x = fma(alpha, pv.x, xv.x);
-    xv.y = fma(alpha, pv.y, xv.y);
-    rv.x = fma(-alpha, av.x, rv.x);
-    rv.y = fma(-alpha, av.y, rv.y);
-    reinterpret_cast<V2 *>(x)[q] = xv;
-    reinterpret_cast<V2 *>(r)[q] = rv;
-    rr = fma(rv.x, rv.x, rr);
-    rr = fma(rv.y, rv.y, rr);
-    if (walls) {
-      const int c0 = cell_class(G, 2 * q), c1 = cell_class(G, 2 * q + 1);
-      if (c0) corr = fma((s_inv[c0] - T(1)) * rv.x, rv.x, corr);
-      if (c1) corr = fma((s_inv[c1] - T(1)) * rv.y, rv.y, corr);
+  const unsigned int stride = gridDim.x * FNT;
+  const unsigned int t0 = blockIdx.x * FNT + threadIdx.x;
+  const unsigned int plane = (unsigned int)G.nx * (unsigned int)G.ny;
+  if (G.px && G.py && !(n & 1) && !(plane & 1)) {
+    // pairs [lo, hi) of the interior planes, then the wall planes
+    const unsigned int wall_lo = G.pz ? 0u : plane / 2;                  // pairs in plane 0
+    const unsigned int wall_hi = G.pz ? n / 2 : (n - plane) / 2;         // first pair of plane nz-1
+    for (unsigned int q = wall_lo + t0; q < wall_hi; q += stride) {
+      const V2 rv = update_pair<T, V2>(q, alpha, x, r, p, Ap);
+      rr = fma(rv.x, rv.x, rr);
+      rr = fma(rv.y, rv.y, rr);
     }
-  }
-  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {  // odd tail
-    const unsigned int c = n - 1;
-    x[c] = fma(alpha, p[c], x[c]);
-    const T rn = fma(-alpha, Ap[c], r[c]);
-    r[c] = rn;
-    rr = fma(rn, rn, rr);
-    const int cl = cell_class(G, c);
-    if (cl) corr = fma((s_inv[cl] - T(1)) * rn, rn, corr);
+    if (!G.pz) {
+      const int wc = 9 * (G.nz == 1 ? 2 : 1);
+      const T w = s_inv[wc] - T(1);
+      for (unsigned int q = t0; q < wall_lo; q += stride) {
+        const V2 rv = update_pair<T, V2>(q, alpha, x, r, p, Ap);
+        const T t = fma(rv.x, rv.x, rv.y * rv.y);
+        rr += t;
+        corr = fma(w, t, corr);
+      }
+      if (G.nz > 1) {
+        for (unsigned int q = wall_hi + t0; q < n / 2; q += stride) {
+          const V2 rv = update_pair<T, V2>(q, alpha, x, r, p, Ap);
+          const T t = fma(rv.x, rv.x, rv.y * rv.y);
+          rr += t;
+          corr = fma(w, t, corr);
+        }
+      }
+    }
+  } else {
+    // general walls: per-cell class
+    for (unsigned int c = t0; c < n; c += stride) {
+      x[c] = fma(alpha, p[c], x[c]);
+      const T rn = fma(-alpha, Ap[c], r[c]);
+      r[c] = rn;
+      rr = fma(rn, rn, rr);
+      const int cl = cell_class(G, c);
+      if (cl) corr = fma((s_inv[cl] - T(1)) * rn, rn, corr);
+    }
   }
   double v[2] = {(double)rr + (double)corr, (double)rr}, tot[2];
   if (last_cta_reduce<2>(v, partials, st, gridDim.x, blockIdx.x, s_red, tot) && threadIdx.x == 0)

@@ -53,8 +53,10 @@ struct bbpp_ctx {
   int sms = 1;
   int kz = 1;          // z planes per stencil CTA (unscaled kernels)
   dim3 sgrid;          // stencil grid (unscaled kernels)
-  int fkz = 1;         // z planes per CTA of the iteration kernels
-  dim3 fgrid;          // grid of the iteration stencil kernels
+  int fkz = 1;         // z planes per CTA of the residual kernel
+  dim3 fgrid;          // grid of the residual kernel (32x16 tiles)
+  int pkz[2] = {1, 1};  // z planes per CTA of the search kernel [FP32, FP64]
+  dim3 pgrid[2];        // grid of the search kernel (64x16 tiles) [FP32, FP64]
   int egrid = 1;       // elementwise grid (1-D)
   size_t nparts = 0;   // capacity of partials (per sum)
   cudaStream_t own_stream = nullptr, stream = nullptr;

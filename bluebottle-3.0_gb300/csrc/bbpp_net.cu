@@ -1,17 +1,954 @@
-// bbpp_net.cu -- learned initial guess (placeholder until the network
-// kernels land): returns BBPP_BAD_ARG.
+// bbpp_net.cu -- the learned initial guess: a small 3D conv encoder-decoder
+// on BF16 tensor cores, trained on the GPU with the library's own forward and
+// backward kernels (bbpp_conv.cuh), and applied before the PCG.
+//
+// Network (channels-last BF16 activations, FP32 master weights, Adam):
+//   X0  [V][16]  = (rhs / s_b, prev / s_p, mask, 0 ...)      s_* = fluid RMS
+//   E1  = relu(conv3(X0;  16 -> 16))      stored in CAT1[:, 32:48]
+//   P1  = avgpool2(E1)                    [V/8][16]
+//   E2  = relu(conv3(P1;  16 -> 32))      stored in CAT2[:, 64:96]
+//   P2  = avgpool2(E2)                    [V/64][32]
+//   E3  = relu(conv3(P2;  32 -> 64))      [V/64][64]
+//   CAT2[:, 0:64] = up2(E3);  D2 = relu(conv3(CAT2; 96 -> 32))   [V/8][32]
+//   CAT1[:, 0:32] = up2(D2);  D1 = relu(conv3(CAT1; 48 -> 16))   [V][16]
+//   OUT = D1 . w_head + b_head  (FP32)    p0 = s_p OUT on fluid cells, 0 on solid
+// Loss: mean over fluid cells of (OUT - p*/s_p)^2.
+// Padding is periodic in x and y and zero in z (the workloads' boundaries).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bbpp.h"
+#include "bbpp_conv.cuh"
 #include "bbpp_internal.h"
 
-int bbpp_net_guess(bbpp_ctx *ctx, void *net, const uint8_t *mask, const double *rhs, const double *prev, double *x,
-                   double *ms) {
-  (void)ctx;
-  (void)net;
-  (void)mask;
-  (void)rhs;
-  (void)prev;
-  (void)x;
-  if (ms) *ms = 0;
-  return BBPP_BAD_ARG;
+using namespace bbnet;
+
+#define NCK(call)                                                                                       \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess) {                                                                            \
+      fprintf(stderr, "bbpp net: %s at %s:%d: %s\n", cudaGetErrorString(e_), __FILE__, __LINE__, #call); \
+      return BBPP_CUDA_ERROR;                                                                           \
+    }                                                                                                   \
+  } while (0)
+
+namespace {
+
+// ------------------------------------------------------------ launchers ---
+template <int CIN, int COUT>
+cudaError_t conv_fwd_t(const ConvArgs &a, cudaStream_t s) {
+  constexpr int smem = conv_fwd_smem<CIN, COUT>();
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3_fwd<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((a.nx + CTX - 1) / CTX, (a.ny + CTY - 1) / CTY, a.nb * ((a.nz + CTZ - 1) / CTZ));
+  k_conv3_fwd<CIN, COUT><<<grid, 256, smem, s>>>(a);
+  return cudaGetLastError();
 }
 
-void bbpp_net_ctx_free(bbpp_ctx *ctx) { (void)ctx; }
+cudaError_t conv_fwd(int cin, int cout, const ConvArgs &a, cudaStream_t s) {
+#define CASE(CI, CO) \
+  if (cin == CI && cout == CO) return conv_fwd_t<CI, CO>(a, s);
+  CASE(16, 16) CASE(16, 32) CASE(32, 64) CASE(96, 32) CASE(48, 16)  // forward layers
+  CASE(16, 48) CASE(32, 96) CASE(64, 32) CASE(32, 16)               // dgrad of the layers
+#undef CASE
+  return cudaErrorInvalidValue;
+}
+
+template <int CIN, int COUT>
+cudaError_t conv_wgrad_t(WgradArgs a, cudaStream_t s) {
+  constexpr int smem = conv_wgrad_smem<CIN, COUT>();
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3_wgrad<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  const long long ntiles = (long long)((a.nx + CTX - 1) / CTX) * ((a.ny + CTY - 1) / CTY) *
+                           ((a.nz + CTZ - 1) / CTZ) * a.nb;
+  int ctas = (int)std::min<long long>(ntiles, 64);
+  a.tiles_per_cta = (int)((ntiles + ctas - 1) / ctas);
+  ctas = (int)((ntiles + a.tiles_per_cta - 1) / a.tiles_per_cta);
+  dim3 grid(ctas, 27);
+  k_conv3_wgrad<CIN, COUT><<<grid, 256, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t conv_wgrad(int cin, int cout, const WgradArgs &a, cudaStream_t s) {
+#define CASE(CI, CO) \
+  if (cin == CI && cout == CO) return conv_wgrad_t<CI, CO>(a, s);
+  CASE(16, 16) CASE(16, 32) CASE(32, 64) CASE(96, 32) CASE(48, 16)
+#undef CASE
+  return cudaErrorInvalidValue;
+}
+
+// W [27][cout][cin] -> Wt [27][cin][cout] with the taps reversed (the dgrad
+// kernel of a 3x3x3 "same" convolution)
+__global__ void k_wflip(const bf16 *__restrict__ w, bf16 *__restrict__ wt, int cin, int cout) {
+  const int n = 27 * cin * cout;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int t = e / (cin * cout), r = e - t * cin * cout;
+    const int ci = r / cout, co = r - ci * cout;
+    wt[e] = w[((26 - t) * cout + co) * cin + ci];
+  }
+}
+
+// ------------------------------------------------------- small kernels ---
+__global__ void k_f32_to_bf16(const float *__restrict__ a, bf16 *__restrict__ b, int n) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+    b[e] = __float2bfloat16_rn(a[e]);
+}
+
+// sum over fluid cells of v^2 for each volume (FP64 atomics, one per CTA)
+template <typename T>
+__global__ void k_fluid_sumsq(const T *__restrict__ v, const uint8_t *__restrict__ mask, long long vol, int nb,
+                              double *out /* [nb][2]: sum v^2, count */) {
+  __shared__ double s1[256], s2[256];
+  const int b = blockIdx.y;
+  double a = 0, c = 0;
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < vol; i += (long long)gridDim.x * 256) {
+    if (mask && mask[i]) continue;
+    const double x = (double)v[(long long)b * vol + i];
+    a += x * x;
+    c += 1;
+  }
+  s1[threadIdx.x] = a;
+  s2[threadIdx.x] = c;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      s1[threadIdx.x] += s1[threadIdx.x + o];
+      s2[threadIdx.x] += s2[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    atomicAdd(&out[2 * b], s1[0]);
+    atomicAdd(&out[2 * b + 1], s2[0]);
+  }
+}
+
+// scales[b] = (1/s_b, 1/s_p) from the sums; s = sqrt(sum/count), 1 if zero
+__global__ void k_scales(const double *sb, const double *sp, int nb, float *scales) {
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const double rb = sb[2 * b + 1] > 0 ? sqrt(sb[2 * b] / sb[2 * b + 1]) : 0;
+    const double rp = sp ? (sp[2 * b + 1] > 0 ? sqrt(sp[2 * b] / sp[2 * b + 1]) : 0) : 0;
+    scales[2 * b] = rb > 0 ? (float)(1.0 / rb) : 1.f;
+    scales[2 * b + 1] = rp > 0 ? (float)(1.0 / rp) : 1.f;
+  }
+}
+
+// X0 = (rhs / s_b, prev / s_p, mask, 0 ...), 16 channels
+template <typename T>
+__global__ void k_prep(const T *__restrict__ rhs, const T *__restrict__ prev, const uint8_t *__restrict__ mask,
+                       const float *__restrict__ scales, long long vol, int nb, bf16 *__restrict__ x0) {
+  const long long n = vol * nb;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
+    const int b = (int)(e / vol);
+    const long long i = e - (long long)b * vol;
+    const bool solid = mask && mask[i];
+    const float r = solid ? 0.f : (float)rhs[e] * scales[2 * b];
+    const float p = (solid || !prev) ? 0.f : (float)prev[e] * scales[2 * b + 1];
+    __nv_bfloat162 *o = reinterpret_cast<__nv_bfloat162 *>(x0 + e * 16);
+    o[0] = __floats2bfloat162_rn(r, p);
+    o[1] = __floats2bfloat162_rn(solid ? 1.f : 0.f, 0.f);
+#pragma unroll
+    for (int q = 2; q < 8; q++) o[q] = __floats2bfloat162_rn(0.f, 0.f);
+  }
+}
+
+// average pool 2x2x2: out[V/8][C] (ld C) from in (ld, off)
+__global__ void k_pool_fwd(const bf16 *__restrict__ in, int ldi, int off, int C, int nx, int ny, int nz, int nb,
+                           bf16 *__restrict__ out) {
+  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
+  const long long n = (long long)hx * hy * hz * nb * C;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
+    const int c = (int)(e % C);
+    long long v = e / C;
+    const int x = (int)(v % hx);
+    v /= hx;
+    const int y = (int)(v % hy);
+    v /= hy;
+    const int z = (int)(v % hz);
+    const int b = (int)(v / hz);
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const long long src = (long long)b * nx * ny * nz + ((long long)(2 * z + (q >> 2)) * ny + 2 * y + ((q >> 1) & 1)) * nx +
+                            2 * x + (q & 1);
+      s += __bfloat162float(in[src * ldi + off + c]);
+    }
+    out[e] = __float2bfloat16_rn(0.125f * s);
+  }
+}
+
+// din[v][c] (ld C) = dskip[v][c] (ld, off; may be null) + dout[parent][c] / 8
+__global__ void k_pool_bwd(const bf16 *__restrict__ dout, const bf16 *__restrict__ dskip, int lds, int offs, int C,
+                           int nx, int ny, int nz, int nb, bf16 *__restrict__ din) {
+  const long long n = (long long)nx * ny * nz * nb * C;
+  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
+    const int c = (int)(e % C);
+    long long v = e / C;
+    const int x = (int)(v % nx);
+    long long t = v / nx;
+    const int y = (int)(t % ny);
+    t /= ny;
+    const int z = (int)(t % nz);
+    const int b = (int)(t / nz);
+    const long long par = (((long long)b * hz + z / 2) * hy + y / 2) * hx + x / 2;
+    float g = 0.125f * __bfloat162float(dout[par * C + c]);
+    if (dskip) g += __bfloat162float(dskip[v * lds + offs + c]);
+    din[e] = __float2bfloat16_rn(g);
+  }
+}
+
+// nearest upsample x2: out[v][off + c] (ld) = in[parent][c] (ld C)
+__global__ void k_up_fwd(const bf16 *__restrict__ in, int C, int nx, int ny, int nz, int nb, bf16 *__restrict__ out,
+                         int ldo, int off) {
+  const long long n = (long long)nx * ny * nz * nb * C;
+  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
+    const int c = (int)(e % C);
+    long long v = e / C;
+    const int x = (int)(v % nx);
+    long long t = v / nx;
+    const int y = (int)(t % ny);
+    t /= ny;
+    const int z = (int)(t % nz);
+    const int b = (int)(t / nz);
+    const long long par = (((long long)b * hz + z / 2) * hy + y / 2) * hx + x / 2;
+    out[v * ldo + off + c] = in[par * C + c];
+  }
+}
+
+// din[p][c] (ld C, at half resolution) = sum of the 8 children dout[v][off + c]
+__global__ void k_up_bwd(const bf16 *__restrict__ dout, int ldo, int off, int C, int nx, int ny, int nz, int nb,
+                         bf16 *__restrict__ din) {
+  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
+  const long long n = (long long)hx * hy * hz * nb * C;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
+    const int c = (int)(e % C);
+    long long v = e / C;
+    const int x = (int)(v % hx);
+    v /= hx;
+    const int y = (int)(v % hy);
+    v /= hy;
+    const int z = (int)(v % hz);
+    const int b = (int)(v / hz);
+    float s = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const long long ch = (long long)b * nx * ny * nz + ((long long)(2 * z + (q >> 2)) * ny + 2 * y + ((q >> 1) & 1)) * nx +
+                           2 * x + (q & 1);
+      s += __bfloat162float(dout[ch * ldo + off + c]);
+    }
+    din[e] = __float2bfloat16_rn(s);
+  }
+}
+
+// g[v][c] (ld C) = dout[v][c] (ld C) * (out[v][off + c] > 0)   (ReLU backward)
+__global__ void k_gate(const bf16 *__restrict__ dout, const bf16 *__restrict__ out, int ldo, int off, int C,
+                       long long nvox, bf16 *__restrict__ g) {
+  const long long n = nvox * C;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
+    const long long v = e / C;
+    const int c = (int)(e - v * C);
+    g[e] = __bfloat162float(out[v * ldo + off + c]) > 0.f ? dout[e] : __float2bfloat16_rn(0.f);
+  }
+}
+
+// db[c] += sum_v g[v][c]
+__global__ void k_bias_grad(const bf16 *__restrict__ g, int C, long long nvox, float *db) {
+  __shared__ float s[256];
+  for (int c = 0; c < C; c++) {
+    float a = 0.f;
+    for (long long v = blockIdx.x * 256LL + threadIdx.x; v < nvox; v += (long long)gridDim.x * 256)
+      a += __bfloat162float(g[v * C + c]);
+    s[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+      if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(&db[c], s[0]);
+    __syncthreads();
+  }
+}
+
+// OUT[v] = D1[v] . w + b   (FP32)
+__global__ void k_head_fwd(const bf16 *__restrict__ d1, const float *__restrict__ w, const float *__restrict__ b,
+                           long long nvox, float *__restrict__ out) {
+  for (long long v = blockIdx.x * 256LL + threadIdx.x; v < nvox; v += (long long)gridDim.x * 256) {
+    float s = b[0];
+    const __nv_bfloat162 *p = reinterpret_cast<const __nv_bfloat162 *>(d1 + v * 16);
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const float2 f = __bfloat1622float2(p[q]);
+      s = fmaf(f.x, w[2 * q], s);
+      s = fmaf(f.y, w[2 * q + 1], s);
+    }
+    out[v] = s;
+  }
+}
+
+// dD1[v][c] = dOUT[v] w[c];  dw[c] += sum_v dOUT[v] D1[v][c];  db += sum dOUT
+__global__ void k_head_bwd(const float *__restrict__ dout, const bf16 *__restrict__ d1, const float *__restrict__ w,
+                           long long nvox, bf16 *__restrict__ dd1, float *dw, float *db) {
+  __shared__ float s[17][257];
+  float a[17];
+#pragma unroll
+  for (int q = 0; q < 17; q++) a[q] = 0.f;
+  for (long long v = blockIdx.x * 256LL + threadIdx.x; v < nvox; v += (long long)gridDim.x * 256) {
+    const float g = dout[v];
+    const __nv_bfloat162 *p = reinterpret_cast<const __nv_bfloat162 *>(d1 + v * 16);
+    __nv_bfloat162 *o = reinterpret_cast<__nv_bfloat162 *>(dd1 + v * 16);
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const float2 f = __bfloat1622float2(p[q]);
+      a[2 * q] += g * f.x;
+      a[2 * q + 1] += g * f.y;
+      o[q] = __floats2bfloat162_rn(g * w[2 * q], g * w[2 * q + 1]);
+    }
+    a[16] += g;
+  }
+#pragma unroll
+  for (int q = 0; q < 17; q++) s[q][threadIdx.x] = a[q];
+  __syncthreads();
+  if (threadIdx.x < 17) {
+    float t = 0.f;
+    for (int i = 0; i < 256; i++) t += s[threadIdx.x][i];
+    if (threadIdx.x < 16) atomicAdd(&dw[threadIdx.x], t);
+    else atomicAdd(db, t);
+  }
+}
+
+// loss = sum over volumes and fluid cells of (OUT - tgt s_p)^2 / nfluid_total;
+// dOUT = 2 (OUT - tgt s_p) / nfluid_total on fluid cells, 0 on solid cells
+__global__ void k_loss(const float *__restrict__ out, const float *__restrict__ tgt, const uint8_t *__restrict__ mask,
+                       const float *__restrict__ scales, long long vol, int nb, double inv_n, float *__restrict__ dout,
+                       double *loss) {
+  __shared__ double s[256];
+  double a = 0;
+  const long long n = vol * nb;
+  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
+    const int b = (int)(e / vol);
+    const long long i = e - (long long)b * vol;
+    if (mask && mask[i]) {
+      dout[e] = 0.f;
+      continue;
+    }
+    const float d = out[e] - tgt[e] * scales[2 * b + 1];
+    a += (double)d * d;
+    dout[e] = (float)(2.0 * inv_n) * d;
+  }
+  s[threadIdx.x] = a;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, s[0] * inv_n);
+}
+
+// p0 = OUT / (1/s_p) on fluid cells, 0 on solid cells
+__global__ void k_guess_out(const float *__restrict__ out, const uint8_t *__restrict__ mask,
+                            const float *__restrict__ scales, long long vol, double *__restrict__ x) {
+  const double sp = 1.0 / (double)scales[1];
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < vol; i += (long long)gridDim.x * 256)
+    x[i] = (mask && mask[i]) ? 0.0 : (double)out[i] * sp;
+}
+
+__global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
+                       int n, float lr, float b1, float b2, float eps, float c1, float c2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  }
+}
+
+int nblocks(long long n) { return (int)std::min<long long>(std::max<long long>((n + 255) / 256, 1), 4096); }
+
+}  // namespace
+
+// ------------------------------------------------------------- network ----
+struct ConvLayer {
+  int cin, cout;
+  int woff, boff;  // offsets in the parameter vector
+};
+
+static const int NLAYER = 5;
+static const ConvLayer kLayers[NLAYER] = {
+    {16, 16, 0, 0}, {16, 32, 0, 0}, {32, 64, 0, 0}, {96, 32, 0, 0}, {48, 16, 0, 0}};
+
+struct bbpp_net {
+  int np = 0;                     // parameters
+  ConvLayer L[NLAYER];
+  int head_w = 0, head_b = 0;
+  float *w = nullptr;             // FP32 master parameters
+  float *g = nullptr;             // gradients
+  float *m = nullptr, *v = nullptr;  // Adam moments
+  bf16 *w16 = nullptr;            // BF16 copy of the parameters (conv weights used from it)
+  bf16 *wt16 = nullptr;           // flipped/transposed conv weights (dgrad)
+  int t = 0;                      // Adam step
+  // workspace for one (nx, ny, nz, nb)
+  int wx = 0, wy = 0, wz = 0, wb = 0;
+  bool wgrad = false;
+  bf16 *X0 = nullptr, *CAT1 = nullptr, *P1 = nullptr, *CAT2 = nullptr, *P2 = nullptr, *E3 = nullptr, *D2 = nullptr,
+       *D1 = nullptr;
+  float *OUT = nullptr, *dOUT = nullptr, *scales = nullptr;
+  double *sums = nullptr, *lossd = nullptr;
+  bf16 *dD1 = nullptr, *G = nullptr, *dCAT1 = nullptr, *dD2 = nullptr, *dCAT2 = nullptr, *dE3 = nullptr,
+       *dP2 = nullptr, *dE2 = nullptr, *dP1 = nullptr, *dE1 = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+static void free_work(bbpp_net *n) {
+  void *ptrs[] = {n->X0, n->CAT1, n->P1, n->CAT2, n->P2, n->E3, n->D2, n->D1, n->OUT, n->dOUT, n->scales, n->sums,
+                  n->lossd, n->dD1, n->G, n->dCAT1, n->dD2, n->dCAT2, n->dE3, n->dP2, n->dE2, n->dP1, n->dE1};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  n->X0 = n->CAT1 = n->P1 = n->CAT2 = n->P2 = n->E3 = n->D2 = n->D1 = nullptr;
+  n->OUT = n->dOUT = n->scales = nullptr;
+  n->sums = n->lossd = nullptr;
+  n->dD1 = n->G = n->dCAT1 = n->dD2 = n->dCAT2 = n->dE3 = n->dP2 = n->dE2 = n->dP1 = n->dE1 = nullptr;
+  n->wx = n->wy = n->wz = n->wb = 0;
+}
+
+static int ensure_work(bbpp_net *n, int nx, int ny, int nz, int nb, bool grads) {
+  if (n->wx == nx && n->wy == ny && n->wz == nz && n->wb == nb && (n->wgrad || !grads)) return 0;
+  free_work(n);
+  const size_t V = (size_t)nx * ny * nz * nb, V2 = V / 8, V4 = V / 64;
+  const size_t B = sizeof(bf16);
+  NCK(cudaMalloc(&n->X0, V * 16 * B));
+  NCK(cudaMalloc(&n->CAT1, V * 48 * B));
+  NCK(cudaMalloc(&n->P1, V2 * 16 * B));
+  NCK(cudaMalloc(&n->CAT2, V2 * 96 * B));
+  NCK(cudaMalloc(&n->P2, V4 * 32 * B));
+  NCK(cudaMalloc(&n->E3, V4 * 64 * B));
+  NCK(cudaMalloc(&n->D2, V2 * 32 * B));
+  NCK(cudaMalloc(&n->D1, V * 16 * B));
+  NCK(cudaMalloc(&n->OUT, V * sizeof(float)));
+  NCK(cudaMalloc(&n->scales, 2 * nb * sizeof(float)));
+  NCK(cudaMalloc(&n->sums, 4 * nb * sizeof(double)));
+  NCK(cudaMalloc(&n->lossd, sizeof(double)));
+  if (grads) {
+    NCK(cudaMalloc(&n->dOUT, V * sizeof(float)));
+    NCK(cudaMalloc(&n->dD1, V * 16 * B));
+    NCK(cudaMalloc(&n->G, V * 32 * B));  // largest gated gradient: [V][16] or [V/8][32] or [V/64][64]
+    NCK(cudaMalloc(&n->dCAT1, V * 48 * B));
+    NCK(cudaMalloc(&n->dD2, V2 * 32 * B));
+    NCK(cudaMalloc(&n->dCAT2, V2 * 96 * B));
+    NCK(cudaMalloc(&n->dE3, V4 * 64 * B));
+    NCK(cudaMalloc(&n->dP2, V4 * 32 * B));
+    NCK(cudaMalloc(&n->dE2, V2 * 32 * B));
+    NCK(cudaMalloc(&n->dP1, V2 * 16 * B));
+    NCK(cudaMalloc(&n->dE1, V * 16 * B));
+  }
+  n->wx = nx;
+  n->wy = ny;
+  n->wz = nz;
+  n->wb = nb;
+  n->wgrad = grads;
+  return 0;
+}
+
+static int check_dims(int nx, int ny, int nz) {
+  if (nx < 4 || ny < 4 || nz < 4 || nx % 4 || ny % 4 || nz % 4) return BBPP_BAD_ARG;
+  return 0;
+}
+
+static ConvArgs cargs(const bbpp_net *n, int nx, int ny, int nz, int nb, const bf16 *in, int ldi, int cio,
+                      const bf16 *w, const float *bias, bf16 *out, int ldo, int coo, int relu) {
+  ConvArgs a;
+  a.in = in;
+  a.ldi = ldi;
+  a.ci_off = cio;
+  a.w = w;
+  a.bias = bias;
+  a.out = out;
+  a.ldo = ldo;
+  a.co_off = coo;
+  a.nx = nx;
+  a.ny = ny;
+  a.nz = nz;
+  a.nb = nb;
+  a.px = 1;
+  a.py = 1;
+  a.pz = 0;
+  a.relu = relu;
+  (void)n;
+  return a;
+}
+
+static WgradArgs wargs(int nx, int ny, int nz, int nb, const bf16 *in, int ldi, int cio, const bf16 *g, int ldg,
+                       float *dW) {
+  WgradArgs a;
+  a.in = in;
+  a.ldi = ldi;
+  a.ci_off = cio;
+  a.g = g;
+  a.ldg = ldg;
+  a.cg_off = 0;
+  a.dW = dW;
+  a.nx = nx;
+  a.ny = ny;
+  a.nz = nz;
+  a.nb = nb;
+  a.px = 1;
+  a.py = 1;
+  a.pz = 0;
+  a.tiles_per_cta = 1;
+  return a;
+}
+
+// refresh the BF16 weight copies after a parameter change
+static int sync_weights(bbpp_net *n) {
+  cudaStream_t s = n->stream;
+  k_f32_to_bf16<<<nblocks(n->np), 256, 0, s>>>(n->w, n->w16, n->np);
+  for (int l = 0; l < NLAYER; l++) {
+    const ConvLayer &L = n->L[l];
+    k_wflip<<<nblocks(27 * L.cin * L.cout), 256, 0, s>>>(n->w16 + L.woff, n->wt16 + L.woff, L.cin, L.cout);
+  }
+  NCK(cudaGetLastError());
+  return 0;
+}
+
+// Forward pass on X0 (already prepared) -> OUT.
+static int forward(bbpp_net *n, int nx, int ny, int nz, int nb) {
+  cudaStream_t s = n->stream;
+  const int hx = nx / 2, hy = ny / 2, hz = nz / 2, qx = nx / 4, qy = ny / 4, qz = nz / 4;
+  const long long V = (long long)nx * ny * nz * nb;
+  const bf16 *W = n->w16;
+  const float *Bf = n->w;
+  const ConvLayer *L = n->L;
+  cudaError_t e;
+  // E1 -> CAT1[:, 32:48]
+  e = conv_fwd(16, 16, cargs(n, nx, ny, nz, nb, n->X0, 16, 0, W + L[0].woff, Bf + L[0].boff, n->CAT1, 48, 32, 1), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  k_pool_fwd<<<nblocks(V / 8 * 16), 256, 0, s>>>(n->CAT1, 48, 32, 16, nx, ny, nz, nb, n->P1);
+  // E2 -> CAT2[:, 64:96]
+  e = conv_fwd(16, 32, cargs(n, hx, hy, hz, nb, n->P1, 16, 0, W + L[1].woff, Bf + L[1].boff, n->CAT2, 96, 64, 1), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  k_pool_fwd<<<nblocks(V / 64 * 32), 256, 0, s>>>(n->CAT2, 96, 64, 32, hx, hy, hz, nb, n->P2);
+  e = conv_fwd(32, 64, cargs(n, qx, qy, qz, nb, n->P2, 32, 0, W + L[2].woff, Bf + L[2].boff, n->E3, 64, 0, 1), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  k_up_fwd<<<nblocks(V / 8 * 64), 256, 0, s>>>(n->E3, 64, hx, hy, hz, nb, n->CAT2, 96, 0);
+  e = conv_fwd(96, 32, cargs(n, hx, hy, hz, nb, n->CAT2, 96, 0, W + L[3].woff, Bf + L[3].boff, n->D2, 32, 0, 1), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  k_up_fwd<<<nblocks(V * 32), 256, 0, s>>>(n->D2, 32, nx, ny, nz, nb, n->CAT1, 48, 0);
+  e = conv_fwd(48, 16, cargs(n, nx, ny, nz, nb, n->CAT1, 48, 0, W + L[4].woff, Bf + L[4].boff, n->D1, 16, 0, 1), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  k_head_fwd<<<nblocks(V), 256, 0, s>>>(n->D1, n->w + n->head_w, n->w + n->head_b, V, n->OUT);
+  NCK(cudaGetLastError());
+  return 0;
+}
+
+// Backward pass from dOUT; accumulates into n->g (which the caller zeroes).
+static int backward(bbpp_net *n, int nx, int ny, int nz, int nb) {
+  cudaStream_t s = n->stream;
+  const int hx = nx / 2, hy = ny / 2, hz = nz / 2, qx = nx / 4, qy = ny / 4, qz = nz / 4;
+  const long long V = (long long)nx * ny * nz * nb, V2 = V / 8, V4 = V / 64;
+  const ConvLayer *L = n->L;
+  float *G32 = n->g;
+  cudaError_t e;
+  k_head_bwd<<<nblocks(V), 256, 0, s>>>(n->dOUT, n->D1, n->w + n->head_w, V, n->dD1, G32 + n->head_w,
+                                        G32 + n->head_b);
+  // D1 = relu(conv(CAT1))
+  k_gate<<<nblocks(V * 16), 256, 0, s>>>(n->dD1, n->D1, 16, 0, 16, V, n->G);
+  k_bias_grad<<<nblocks(V) / 8 + 1, 256, 0, s>>>(n->G, 16, V, G32 + L[4].boff);
+  e = conv_wgrad(48, 16, wargs(nx, ny, nz, nb, n->CAT1, 48, 0, n->G, 16, G32 + L[4].woff), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  e = conv_fwd(16, 48, cargs(n, nx, ny, nz, nb, n->G, 16, 0, n->wt16 + L[4].woff, nullptr, n->dCAT1, 48, 0, 0), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  // CAT1[:, 0:32] = up(D2)
+  k_up_bwd<<<nblocks(V2 * 32), 256, 0, s>>>(n->dCAT1, 48, 0, 32, nx, ny, nz, nb, n->dD2);
+  // D2 = relu(conv(CAT2))
+  k_gate<<<nblocks(V2 * 32), 256, 0, s>>>(n->dD2, n->D2, 32, 0, 32, V2, n->G);
+  k_bias_grad<<<nblocks(V2) / 8 + 1, 256, 0, s>>>(n->G, 32, V2, G32 + L[3].boff);
+  e = conv_wgrad(96, 32, wargs(hx, hy, hz, nb, n->CAT2, 96, 0, n->G, 32, G32 + L[3].woff), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  e = conv_fwd(32, 96, cargs(n, hx, hy, hz, nb, n->G, 32, 0, n->wt16 + L[3].woff, nullptr, n->dCAT2, 96, 0, 0), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  // CAT2[:, 0:64] = up(E3)
+  k_up_bwd<<<nblocks(V4 * 64), 256, 0, s>>>(n->dCAT2, 96, 0, 64, hx, hy, hz, nb, n->dE3);
+  // E3 = relu(conv(P2))
+  k_gate<<<nblocks(V4 * 64), 256, 0, s>>>(n->dE3, n->E3, 64, 0, 64, V4, n->G);
+  k_bias_grad<<<nblocks(V4) / 8 + 1, 256, 0, s>>>(n->G, 64, V4, G32 + L[2].boff);
+  e = conv_wgrad(32, 64, wargs(qx, qy, qz, nb, n->P2, 32, 0, n->G, 64, G32 + L[2].woff), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  e = conv_fwd(64, 32, cargs(n, qx, qy, qz, nb, n->G, 64, 0, n->wt16 + L[2].woff, nullptr, n->dP2, 32, 0, 0), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  // E2 (in CAT2[:, 64:96]): skip gradient dCAT2[:, 64:96] + pool backward of dP2
+  k_pool_bwd<<<nblocks(V2 * 32), 256, 0, s>>>(n->dP2, n->dCAT2, 96, 64, 32, hx, hy, hz, nb, n->dE2);
+  k_gate<<<nblocks(V2 * 32), 256, 0, s>>>(n->dE2, n->CAT2, 96, 64, 32, V2, n->G);
+  k_bias_grad<<<nblocks(V2) / 8 + 1, 256, 0, s>>>(n->G, 32, V2, G32 + L[1].boff);
+  e = conv_wgrad(16, 32, wargs(hx, hy, hz, nb, n->P1, 16, 0, n->G, 32, G32 + L[1].woff), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  e = conv_fwd(32, 16, cargs(n, hx, hy, hz, nb, n->G, 32, 0, n->wt16 + L[1].woff, nullptr, n->dP1, 16, 0, 0), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  // E1 (in CAT1[:, 32:48]): skip gradient dCAT1[:, 32:48] + pool backward of dP1
+  k_pool_bwd<<<nblocks(V * 16), 256, 0, s>>>(n->dP1, n->dCAT1, 48, 32, 16, nx, ny, nz, nb, n->dE1);
+  k_gate<<<nblocks(V * 16), 256, 0, s>>>(n->dE1, n->CAT1, 48, 32, 16, V, n->G);
+  k_bias_grad<<<nblocks(V) / 8 + 1, 256, 0, s>>>(n->G, 16, V, G32 + L[0].boff);
+  e = conv_wgrad(16, 16, wargs(nx, ny, nz, nb, n->X0, 16, 0, n->G, 16, G32 + L[0].woff), s);
+  if (e != cudaSuccess) return BBPP_CUDA_ERROR;
+  NCK(cudaGetLastError());
+  return 0;
+}
+
+// scales from rhs and (optionally) prev, then X0
+template <typename T>
+static int prepare(bbpp_net *n, int nx, int ny, int nz, int nb, const T *rhs, const T *prev, const uint8_t *mask) {
+  cudaStream_t s = n->stream;
+  const long long vol = (long long)nx * ny * nz;
+  NCK(cudaMemsetAsync(n->sums, 0, 4 * nb * sizeof(double), s));
+  dim3 g(std::min(nblocks(vol), 512), nb);
+  k_fluid_sumsq<T><<<g, 256, 0, s>>>(rhs, mask, vol, nb, n->sums);
+  if (prev) k_fluid_sumsq<T><<<g, 256, 0, s>>>(prev, mask, vol, nb, n->sums + 2 * nb);
+  k_scales<<<1, 256, 0, s>>>(n->sums, prev ? n->sums + 2 * nb : nullptr, nb, n->scales);
+  k_prep<T><<<nblocks(vol * nb), 256, 0, s>>>(rhs, prev, mask, n->scales, vol, nb, n->X0);
+  NCK(cudaGetLastError());
+  return 0;
+}
+
+// ------------------------------------------------------------------- ABI --
+static unsigned long long rng_next(unsigned long long &v) {  // Ranq1 (src/rng.c:28-51)
+  v ^= v >> 21;
+  v ^= v << 35;
+  v ^= v >> 4;
+  return v * 2685821657736338717ULL;
+}
+
+extern "C" int bbpp_net_create(unsigned long long seed, bbpp_net **out) {
+  if (!out) return BBPP_BAD_ARG;
+  bbpp_net *n = new bbpp_net();
+  int off = 0;
+  for (int l = 0; l < NLAYER; l++) {
+    n->L[l] = kLayers[l];
+    n->L[l].woff = off;
+    off += 27 * n->L[l].cin * n->L[l].cout;
+    n->L[l].boff = off;
+    off += n->L[l].cout;
+  }
+  n->head_w = off;
+  off += 16;
+  n->head_b = off;
+  off += 1;
+  n->np = off;
+  // He-uniform initialisation from Ranq1; biases zero; the real input
+  // channels of the first layer are 3 of its 16
+  std::vector<float> h(n->np, 0.f);
+  unsigned long long v = 4101842887655102017ULL ^ seed;
+  rng_next(v);
+  for (int l = 0; l < NLAYER; l++) {
+    const ConvLayer &L = n->L[l];
+    const int fan_in = 27 * (l == 0 ? 3 : L.cin);
+    const float bound = sqrtf(6.f / fan_in);
+    for (int t = 0; t < 27; t++)
+      for (int co = 0; co < L.cout; co++)
+        for (int ci = 0; ci < L.cin; ci++) {
+          const double u = 5.42101086242752217e-20 * (double)rng_next(v);
+          const float val = (l == 0 && ci >= 3) ? 0.f : (float)((2 * u - 1) * bound);
+          h[L.woff + (t * L.cout + co) * L.cin + ci] = val;
+        }
+  }
+  for (int c = 0; c < 16; c++) {
+    const double u = 5.42101086242752217e-20 * (double)rng_next(v);
+    h[n->head_w + c] = (float)((2 * u - 1) * sqrtf(6.f / 16.f) * 0.1f);
+  }
+  cudaError_t e = cudaMalloc(&n->w, n->np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&n->g, n->np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&n->m, n->np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&n->v, n->np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&n->w16, n->np * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&n->wt16, n->np * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMemcpy(n->w, h.data(), n->np * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(n->g, 0, n->np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(n->m, 0, n->np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(n->v, 0, n->np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(n->wt16, 0, n->np * sizeof(bf16));
+  if (e != cudaSuccess) {
+    fprintf(stderr, "bbpp_net_create: %s\n", cudaGetErrorString(e));
+    bbpp_net_destroy(n);
+    return BBPP_CUDA_ERROR;
+  }
+  int rc = sync_weights(n);
+  if (rc) {
+    bbpp_net_destroy(n);
+    return rc;
+  }
+  cudaDeviceSynchronize();
+  *out = n;
+  return 0;
+}
+
+extern "C" int bbpp_net_destroy(bbpp_net *n) {
+  if (!n) return BBPP_BAD_ARG;
+  free_work(n);
+  void *ptrs[] = {n->w, n->g, n->m, n->v, n->w16, n->wt16};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete n;
+  return 0;
+}
+
+extern "C" int bbpp_net_num_params(const bbpp_net *n) { return n ? n->np : 0; }
+
+extern "C" int bbpp_net_get_params(const bbpp_net *n, float *host) {
+  if (!n || !host) return BBPP_BAD_ARG;
+  NCK(cudaMemcpy(host, n->w, n->np * sizeof(float), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int bbpp_net_set_params(bbpp_net *n, const float *host) {
+  if (!n || !host) return BBPP_BAD_ARG;
+  NCK(cudaMemcpy(n->w, host, n->np * sizeof(float), cudaMemcpyHostToDevice));
+  int rc = sync_weights(n);
+  if (rc) return rc;
+  NCK(cudaStreamSynchronize(n->stream));
+  return 0;
+}
+
+// Forward (FP32 inputs), loss and gradients: loss to *loss, gradients to grads
+// (host, np floats) when not null.  Volumes of nx*ny*nz stacked nb times;
+// mask (one volume) may be null.
+extern "C" int bbpp_net_loss_grad(bbpp_net *n, int nx, int ny, int nz, int nb, const float *rhs, const float *prev,
+                                  const float *target, const uint8_t *mask, double *loss, float *grads) {
+  if (!n || !rhs || !target || nb < 1) return BBPP_BAD_ARG;
+  int rc = check_dims(nx, ny, nz);
+  if (rc) return rc;
+  rc = ensure_work(n, nx, ny, nz, nb, true);
+  if (rc) return rc;
+  rc = prepare<float>(n, nx, ny, nz, nb, rhs, prev, mask);
+  if (rc) return rc;
+  rc = forward(n, nx, ny, nz, nb);
+  if (rc) return rc;
+  cudaStream_t s = n->stream;
+  const long long vol = (long long)nx * ny * nz;
+  // fluid count over all volumes
+  long long nfl = vol;
+  if (mask) {
+    std::vector<uint8_t> hm(vol);
+    NCK(cudaMemcpy(hm.data(), mask, vol, cudaMemcpyDeviceToHost));
+    nfl = 0;
+    for (long long i = 0; i < vol; i++) nfl += hm[i] == 0;
+  }
+  const double inv_n = 1.0 / std::max<long long>(1, nfl * nb);
+  NCK(cudaMemsetAsync(n->lossd, 0, sizeof(double), s));
+  k_loss<<<std::min(nblocks(vol * nb), 1024), 256, 0, s>>>(n->OUT, target, mask, n->scales, vol, nb, inv_n, n->dOUT,
+                                                            n->lossd);
+  NCK(cudaMemsetAsync(n->g, 0, n->np * sizeof(float), s));
+  rc = backward(n, nx, ny, nz, nb);
+  if (rc) return rc;
+  if (loss) NCK(cudaMemcpyAsync(loss, n->lossd, sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (grads) NCK(cudaMemcpyAsync(grads, n->g, n->np * sizeof(float), cudaMemcpyDeviceToHost, s));
+  NCK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+// Train on a device-resident set of nsamples volumes (FP32 rhs, prev, target;
+// one shared mask): `steps` Adam steps on batches of `batch` volumes drawn
+// with Ranq1.  loss_hist (host, steps) may be null.
+extern "C" int bbpp_net_train(bbpp_net *n, int nx, int ny, int nz, int nsamples, const float *rhs, const float *prev,
+                              const float *target, const uint8_t *mask, int steps, int batch, float lr,
+                              unsigned long long seed, float *loss_hist) {
+  if (!n || !rhs || !target || nsamples < 1 || batch < 1 || steps < 0) return BBPP_BAD_ARG;
+  int rc = check_dims(nx, ny, nz);
+  if (rc) return rc;
+  const long long vol = (long long)nx * ny * nz;
+  float *brhs = nullptr, *bprev = nullptr, *btgt = nullptr;
+  NCK(cudaMalloc(&brhs, vol * batch * sizeof(float)));
+  NCK(cudaMalloc(&bprev, vol * batch * sizeof(float)));
+  NCK(cudaMalloc(&btgt, vol * batch * sizeof(float)));
+  unsigned long long v = 4101842887655102017ULL ^ seed;
+  rng_next(v);
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int it = 0; it < steps; it++) {
+    for (int b = 0; b < batch; b++) {
+      const int k = (int)(rng_next(v) % (unsigned long long)nsamples);
+      NCK(cudaMemcpyAsync(brhs + b * vol, rhs + k * vol, vol * sizeof(float), cudaMemcpyDeviceToDevice, n->stream));
+      if (prev)
+        NCK(cudaMemcpyAsync(bprev + b * vol, prev + k * vol, vol * sizeof(float), cudaMemcpyDeviceToDevice,
+                            n->stream));
+      NCK(cudaMemcpyAsync(btgt + b * vol, target + k * vol, vol * sizeof(float), cudaMemcpyDeviceToDevice,
+                          n->stream));
+    }
+    double loss = 0;
+    rc = bbpp_net_loss_grad(n, nx, ny, nz, batch, brhs, prev ? bprev : nullptr, btgt, mask, &loss, nullptr);
+    if (rc) break;
+    n->t++;
+    const float c1 = 1.f / (1.f - powf(b1, (float)n->t)), c2 = 1.f / (1.f - powf(b2, (float)n->t));
+    // cosine decay of the learning rate
+    const float lrt = lr * 0.5f * (1.f + cosf(3.14159265f * (float)it / (float)std::max(1, steps)));
+    k_adam<<<nblocks(n->np), 256, 0, n->stream>>>(n->w, n->g, n->m, n->v, n->np, lrt, b1, b2, eps, c1, c2);
+    rc = sync_weights(n);
+    if (rc) break;
+    if (loss_hist) loss_hist[it] = (float)loss;
+  }
+  cudaStreamSynchronize(n->stream);
+  cudaFree(brhs);
+  cudaFree(bprev);
+  cudaFree(btgt);
+  return rc;
+}
+
+// Inference for one volume (FP64 rhs / prev as the solver holds them) into
+// p0 (FP64): p0 = s_p OUT on fluid cells, 0 on solid cells.
+extern "C" int bbpp_net_infer(bbpp_net *n, int nx, int ny, int nz, const double *rhs, const double *prev,
+                              const uint8_t *mask, double *p0) {
+  if (!n || !rhs || !p0) return BBPP_BAD_ARG;
+  int rc = check_dims(nx, ny, nz);
+  if (rc) return rc;
+  rc = ensure_work(n, nx, ny, nz, 1, false);
+  if (rc) return rc;
+  rc = prepare<double>(n, nx, ny, nz, 1, rhs, prev, mask);
+  if (rc) return rc;
+  rc = forward(n, nx, ny, nz, 1);
+  if (rc) return rc;
+  const long long vol = (long long)nx * ny * nz;
+  k_guess_out<<<nblocks(vol), 256, 0, n->stream>>>(n->OUT, mask, n->scales, vol, p0);
+  NCK(cudaGetLastError());
+  return 0;
+}
+
+extern "C" int bbpp_net_set_stream(bbpp_net *n, void *stream) {
+  if (!n) return BBPP_BAD_ARG;
+  n->stream = (cudaStream_t)stream;
+  return 0;
+}
+
+extern "C" int bbpp_net_save(const bbpp_net *n, const char *path) {
+  if (!n || !path) return BBPP_BAD_ARG;
+  std::vector<float> h(3 * (size_t)n->np);
+  NCK(cudaMemcpy(h.data(), n->w, n->np * sizeof(float), cudaMemcpyDeviceToHost));
+  NCK(cudaMemcpy(h.data() + n->np, n->m, n->np * sizeof(float), cudaMemcpyDeviceToHost));
+  NCK(cudaMemcpy(h.data() + 2 * n->np, n->v, n->np * sizeof(float), cudaMemcpyDeviceToHost));
+  FILE *f = fopen(path, "wb");
+  if (!f) return BBPP_BAD_ARG;
+  const char magic[8] = {'B', 'B', 'P', 'P', 'N', 'E', 'T', '1'};
+  fwrite(magic, 1, 8, f);
+  fwrite(&n->np, sizeof(int), 1, f);
+  fwrite(&n->t, sizeof(int), 1, f);
+  fwrite(h.data(), sizeof(float), h.size(), f);
+  fclose(f);
+  return 0;
+}
+
+extern "C" int bbpp_net_load(bbpp_net *n, const char *path) {
+  if (!n || !path) return BBPP_BAD_ARG;
+  FILE *f = fopen(path, "rb");
+  if (!f) return BBPP_BAD_ARG;
+  char magic[8];
+  int np = 0, t = 0;
+  std::vector<float> h(3 * (size_t)n->np);
+  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, "BBPPNET1", 8) == 0 && fread(&np, sizeof(int), 1, f) == 1 &&
+            np == n->np && fread(&t, sizeof(int), 1, f) == 1 && fread(h.data(), sizeof(float), h.size(), f) == h.size();
+  fclose(f);
+  if (!ok) return BBPP_BAD_ARG;
+  NCK(cudaMemcpy(n->w, h.data(), n->np * sizeof(float), cudaMemcpyHostToDevice));
+  NCK(cudaMemcpy(n->m, h.data() + n->np, n->np * sizeof(float), cudaMemcpyHostToDevice));
+  NCK(cudaMemcpy(n->v, h.data() + 2 * n->np, n->np * sizeof(float), cudaMemcpyHostToDevice));
+  n->t = t;
+  int rc = sync_weights(n);
+  if (rc) return rc;
+  NCK(cudaDeviceSynchronize());
+  return 0;
+}
+
+// Kernel-level entry points for tests: one 3x3x3 convolution (forward, or
+// dgrad with `flip`), and a weight gradient, on BF16 channels-last volumes.
+extern "C" int bbpp_conv3(int cin, int cout, const void *in, int ldi, int ci_off, const void *w, const float *bias,
+                          void *out, int ldo, int co_off, int nx, int ny, int nz, int nb, int px, int py, int pz,
+                          int relu) {
+  ConvArgs a;
+  a.in = (const bf16 *)in;
+  a.ldi = ldi;
+  a.ci_off = ci_off;
+  a.w = (const bf16 *)w;
+  a.bias = bias;
+  a.out = (bf16 *)out;
+  a.ldo = ldo;
+  a.co_off = co_off;
+  a.nx = nx;
+  a.ny = ny;
+  a.nz = nz;
+  a.nb = nb;
+  a.px = px;
+  a.py = py;
+  a.pz = pz;
+  a.relu = relu;
+  if (ldi % 8 || ci_off % 8 || ldo % 2 || co_off % 2 || nb < 1 || nx < 1 || ny < 1 || nz < 1) return BBPP_BAD_ARG;
+  if (conv_fwd(cin, cout, a, 0) != cudaSuccess) return BBPP_BAD_ARG;
+  NCK(cudaDeviceSynchronize());
+  return 0;
+}
+
+extern "C" int bbpp_conv3_wgrad(int cin, int cout, const void *in, int ldi, int ci_off, const void *g, int ldg,
+                                float *dW, int nx, int ny, int nz, int nb, int px, int py, int pz) {
+  WgradArgs a = wargs(nx, ny, nz, nb, (const bf16 *)in, ldi, ci_off, (const bf16 *)g, ldg, dW);
+  a.px = px;
+  a.py = py;
+  a.pz = pz;
+  if (ldi % 8 || ci_off % 8 || ldg % 8 || nb < 1) return BBPP_BAD_ARG;
+  if (conv_wgrad(cin, cout, a, 0) != cudaSuccess) return BBPP_BAD_ARG;
+  NCK(cudaDeviceSynchronize());
+  return 0;
+}
+
+extern "C" int bbpp_conv3_wflip(int cin, int cout, const void *w, void *wt) {
+  k_wflip<<<nblocks(27 * cin * cout), 256>>>((const bf16 *)w, (bf16 *)wt, cin, cout);
+  NCK(cudaGetLastError());
+  NCK(cudaDeviceSynchronize());
+  return 0;
+}
+
+// ------------------------------------------------------ solver hook -------
+struct NetWork {
+  double *prev0 = nullptr;  // zero "previous pressure" when none is given
+};
+
+int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double *rhs, const double *prev, double *x,
+                   double *ms) {
+  bbpp_net *n = (bbpp_net *)netp;
+  if (!n) return BBPP_BAD_ARG;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaStream_t saved = n->stream;
+  n->stream = ctx->stream;
+  cudaEventRecord(e0, ctx->stream);
+  int rc = bbpp_net_infer(n, ctx->G.nx, ctx->G.ny, ctx->G.nz, rhs, prev, mask, x);
+  cudaEventRecord(e1, ctx->stream);
+  n->stream = saved;
+  if (rc == 0) {
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    if (ms) *ms = t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+void bbpp_net_ctx_free(bbpp_ctx *ctx) {
+  if (ctx && ctx->net) {
+    if (ctx->net->prev0) cudaFree(ctx->net->prev0);
+    delete ctx->net;
+    ctx->net = nullptr;
+  }
+}

@@ -176,6 +176,41 @@ int bbpp_kernel_stats(bbpp_ctx *ctx, bbpp_kstat *out, int max, int *n);
  * counters; events are captured between the kernels of the graphs. */
 int bbpp_set_profiling(bbpp_ctx *ctx, int on);
 
+/* ---- learned initial guess (no counterpart in the reference) ----
+ * A 3-level 3D conv encoder-decoder (channels 16/32/64, 3x3x3 kernels, BF16
+ * activations and tensor-core convolutions with FP32 accumulation, FP32
+ * master weights, Adam) that maps (rhs, previous pressure, phase mask) to an
+ * initial guess p0.  Volumes need sizes divisible by 4; padding is periodic in
+ * x and y and zero in z.  All array arguments are device pointers. */
+typedef struct bbpp_net bbpp_net;
+int bbpp_net_create(unsigned long long seed, bbpp_net **out);
+int bbpp_net_destroy(bbpp_net *net);
+int bbpp_net_num_params(const bbpp_net *net);
+int bbpp_net_get_params(const bbpp_net *net, float *host);
+int bbpp_net_set_params(bbpp_net *net, const float *host);
+/* Loss (mean over fluid cells of (out - target/s_p)^2) and its gradient
+ * (host array of num_params floats, may be NULL) for nb stacked volumes. */
+int bbpp_net_loss_grad(bbpp_net *net, int nx, int ny, int nz, int nb, const float *rhs, const float *prev,
+                       const float *target, const uint8_t *mask, double *loss, float *grads_host);
+/* Adam training on nsamples device-resident volumes (batches drawn by Ranq1). */
+int bbpp_net_train(bbpp_net *net, int nx, int ny, int nz, int nsamples, const float *rhs, const float *prev,
+                   const float *target, const uint8_t *mask, int steps, int batch, float lr,
+                   unsigned long long seed, float *loss_hist_host);
+/* p0 (FP64) from rhs and prev (FP64, prev may be NULL) for one volume. */
+int bbpp_net_infer(bbpp_net *net, int nx, int ny, int nz, const double *rhs, const double *prev,
+                   const uint8_t *mask, double *p0);
+int bbpp_net_set_stream(bbpp_net *net, void *stream);
+int bbpp_net_save(const bbpp_net *net, const char *path);
+int bbpp_net_load(bbpp_net *net, const char *path);
+/* One 3x3x3 convolution on BF16 channels-last volumes (w: [27][cout][cin]);
+ * the weight gradient dW += sum_v g[v]^T in[v + tap] (FP32 [27][cout][cin]);
+ * and the flipped transpose of w used for the input gradient. */
+int bbpp_conv3(int cin, int cout, const void *in, int ldi, int ci_off, const void *w, const float *bias,
+               void *out, int ldo, int co_off, int nx, int ny, int nz, int nb, int px, int py, int pz, int relu);
+int bbpp_conv3_wgrad(int cin, int cout, const void *in, int ldi, int ci_off, const void *g, int ldg, float *dW,
+                     int nx, int ny, int nz, int nb, int px, int py, int pz);
+int bbpp_conv3_wflip(int cin, int cout, const void *w, void *wt);
+
 /* Ranq1 generator (src/rng.c:25-107), for reproducible synthetic inputs. */
 void bbpp_rng_uniform(unsigned long long seed, long long n, double lo, double hi, double *out);
 void bbpp_rng_gauss(unsigned long long seed, long long n, double *out);
