@@ -25,7 +25,8 @@ sys.path.insert(0, os.path.join(ROOT, "bluebottle-3.0_gb300"))
 
 METRIC = "256³ Poisson time-to-1e-8 residual: learned+mixed vs plain FP64 PCG, one GB300"
 UNIT = "solves/s"
-WORKLOAD = "C3: 256^3 cells, periodic x/y + Neumann z, 1000 spheres r=6 cells, k^-11/3 RHS, tol 1e-8 (true rel.)"
+WORKLOAD = ("C3: 256^3 cells, periodic x/y + Neumann z, 1000 spheres r=6 cells, k^-11/3 RHS (step 1 of an OU "
+            "sequence), tol 1e-8 (true rel.)")
 # Plain FP64 PCG iterations of the C3 workload to 1e-8 (seed 3), measured by
 # the CUDA path and equal to the oracle's count; used to scale the bounded CPU
 # sample of the reference arm to a full solve.
@@ -118,6 +119,32 @@ def make_c3():
     return g, cents, radii, c
 
 
+def train_c4_net(args):
+    """The learned guess per the C4 workload: OU triples at 64^3 (128 spheres of
+    radius 4 cells), p* by plain FP64 PCG to 1e-10, Adam on the GPU.  A saved
+    network (--net) skips the training."""
+    from bbpp import learned, problems
+    net = learned.Net(seed=1)
+    info = {}
+    if args.net and os.path.exists(args.net):
+        net.load(args.net)
+        info["loaded"] = args.net
+        return net, info
+    c = problems.CONFIGS["C4"]
+    t0 = time.time()
+    data, g4, _ = learned.make_ou_dataset(c["n"], args.train_samples, nsph=c["nsph"], rad=c["rad"], seed=c["seed"],
+                                          tol=c["tol"])
+    t1 = time.time()
+    hist = net.train(data, steps=args.train_steps, batch=4, lr=2e-3)
+    import numpy as np
+    info = {"samples": args.train_samples, "steps": args.train_steps, "data_s": round(t1 - t0, 1),
+            "train_s": round(time.time() - t1, 1), "loss_first": float(np.mean(hist[:10])),
+            "loss_last": float(np.mean(hist[-50:]))}
+    if args.net:
+        net.save(args.net)
+    return net, info
+
+
 def cpu_sample(g, rhs, mask, iters_full, threads):
     """Time the oracle PCG on the full-size workload for a bounded number of
     iterations and scale to a full solve: t = t_setup + t_iter * iters_full."""
@@ -149,7 +176,9 @@ def run_reference(args):
     from bbpp import problems
     g, cents, radii, c = make_c3()
     mask = problems.sphere_mask_host(g, cents, radii)
-    rhs = problems.spectral_rhs(g.shape, c["seed"], mask)
+    seq = problems.OUSequence(g.shape, c["seed"], mask)
+    seq.field()
+    rhs = seq.step()  # the same right-hand side as the GPU arm
     threads = os.cpu_count() or 1
     iters = args.ref_iters
     vals = []
@@ -180,18 +209,37 @@ def run_ours(args):
     dmask = bbpp.DeviceArray(g.shape, np.uint8)
     s.sphere_mask(cents, radii, dmask)
     mask = dmask.download()
-    rhs = problems.spectral_rhs(g.shape, c["seed"], mask)
-    drhs = bbpp.DeviceArray.from_host(rhs)
+    # the solve at step t of an OU sequence on the C3 geometry; step t-1 gives
+    # the previous pressure the learned guess starts from
+    seq = problems.OUSequence(g.shape, c["seed"], mask)
+    rhs_prev = seq.field()
+    rhs = seq.step()
+    drhs = bbpp.DeviceArray.from_host(rhs_prev)
+    dprev = bbpp.DeviceArray(g.shape, np.float64)
+    s.solve(drhs, dprev, dmask, tol=1e-10, precision=bbpp.FP64)
+    drhs.upload(rhs)
     dx = bbpp.DeviceArray(g.shape, np.float64)
     N = g.n
     tol = c["tol"]
 
-    methods = {"fp64": dict(precision=bbpp.FP64), "ir": dict(precision=bbpp.FP32_IR)}
+    net = None
+    net_info = None
+    methods = {"fp64": dict(precision=bbpp.FP64), "ir": dict(precision=bbpp.FP32_IR),
+               "ir_warm": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_GIVEN)}
     headline = "ir"
+    if not args.no_learned and not args.only:
+        net, net_info = train_c4_net(args)
+        methods["learned_ir"] = dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle,
+                                     prev=dprev.ptr)
+        headline = "learned_ir"
 
     def step(kw):
+        if kw.get("guess") == bbpp.GUESS_GIVEN:
+            dx.upload(prev_host)  # warm start: x = p_prev before the (timed) solve
         bbpp.flush_l2()
         return s.solve(drhs, dx, dmask, tol=tol, **kw)
+
+    prev_host = dprev.download()
 
     if args.only:
         # solves of one method only (profiler runs): steps solves, no warm-up
@@ -242,11 +290,16 @@ def run_ours(args):
     hm.array[...] = mask
     e2e_t = []
     o = bbpp.default_opts(tol=tol, **methods[headline])
+    hp = bbpp.PinnedArray(g.shape, np.float64)
+    hp.array[...] = prev_host
     import ctypes
     for i in range(args.warmup + args.steps):
         rep = bbpp.Report()
         bbpp.flush_l2()
         t0 = time.perf_counter()
+        # the previous pressure also comes from the host (pinned) for the learned guess
+        if headline == "learned_ir":
+            bbpp.lib().bbpp_h2d(dprev.ptr, hp.ptr, N * 8)
         rc = bbpp.lib().bbpp_solve_host(s.handle, hm.ptr, hr.ptr, hx.ptr, ctypes.byref(o), ctypes.byref(rep))
         t1 = time.perf_counter()
         assert rc == bbpp.CONVERGED, rc
@@ -292,6 +345,7 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32-inner/f64-refined" if headline == "ir" else "f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "method": {"ir": "FP32-inner / FP64-refined Jacobi PCG",
+                                                     "learned_ir": "learned guess (C4 net) + FP32-inner / FP64-refined PCG",
                                                      "fp64": "plain FP64 Jacobi PCG"}[headline],
                    "l2": "flushed (512 MB write) before every step; working set 0.9 GB > L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -302,8 +356,12 @@ def run_ours(args):
         "speedup_vs_plain_fp64": plain["ms"] / H["ms"],
         "canonical_gbs": canon_gbs(H),
         "roofline": roof(headline),
-        "e2e": {"value": e2e_v, "unit": UNIT, "h2d_bytes_per_step": int(N * 9), "d2h_bytes_per_step": int(N * 8),
-                "max_abs_diff_vs_device": None},
+        "e2e": {"value": e2e_v, "unit": UNIT,
+                "h2d_bytes_per_step": int(N * 9 + (N * 8 if headline == "learned_ir" else 0)),
+                "d2h_bytes_per_step": int(N * 8)},
+        "methods": {k: {"ms": v["ms"], "iters": v["iters"], "outer": v["outer"], "true_rel": v["true_rel"],
+                        "solves_per_s": 1000.0 / v["ms"]} for k, v in res.items()},
+        "learned_training": net_info,
         "gpu_launches": H["launches"],
         "clocks": clk,
         "cpu_baseline": cpu,
@@ -319,6 +377,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-learned", action="store_true", help="skip training / timing the learned guess")
+    ap.add_argument("--net", default=None, help="load (or save after training) the learned-guess network here")
+    ap.add_argument("--train-samples", type=int, default=2000)
+    ap.add_argument("--train-steps", type=int, default=1500)
     ap.add_argument("--only", default=None, choices=["fp64", "ir"],
                     help="run only warm-up + steps solves of one method (profiler runs)")
     ap.add_argument("--ref-iters", type=int, default=0,

@@ -28,9 +28,9 @@ def _sig():
         "bbpp_net_num_params": (I, [P]),
         "bbpp_net_get_params": (I, [P, P]),
         "bbpp_net_set_params": (I, [P, P]),
-        "bbpp_net_loss_grad": (I, [P, I, I, I, I, P, P, P, P, ctypes.POINTER(D), P]),
-        "bbpp_net_train": (I, [P, I, I, I, I, P, P, P, P, I, I, F, ctypes.c_ulonglong, P]),
-        "bbpp_net_infer": (I, [P, I, I, I, P, P, P, P]),
+        "bbpp_net_loss_grad": (I, [P, I, I, I, I, D, P, P, P, P, ctypes.POINTER(D), P]),
+        "bbpp_net_train": (I, [P, I, I, I, I, D, P, P, P, P, I, I, F, ctypes.c_ulonglong, P]),
+        "bbpp_net_infer": (I, [P, I, I, I, D, P, P, P, P]),
         "bbpp_net_save": (I, [P, ctypes.c_char_p]),
         "bbpp_net_load": (I, [P, ctypes.c_char_p]),
         "bbpp_conv3": (I, [I, I, P, I, I, P, P, P, I, I, I, I, I, I, I, I, I, I]),
@@ -82,26 +82,27 @@ class Net:
         p = np.ascontiguousarray(p, dtype=np.float32)
         _check(_sig().bbpp_net_set_params(self.handle, p.ctypes.data))
 
-    def loss_grad(self, dims, rhs, prev, target, mask=None, grads=True):
-        """dims = (nx, ny, nz); rhs/prev/target DeviceArrays of nb stacked volumes."""
+    def loss_grad(self, dims, h2, r, prev, target, mask=None, grads=True):
+        """dims = (nx, ny, nz); r (residual of prev), prev, target (p* - prev):
+        DeviceArrays of nb stacked FP32 volumes; h2 the squared spacing."""
         nx, ny, nz = dims
-        nb = rhs.nbytes // (4 * nx * ny * nz)
+        nb = r.nbytes // (4 * nx * ny * nz)
         loss = ctypes.c_double()
         g = np.empty(self.num_params, np.float32) if grads else None
-        _check(_sig().bbpp_net_loss_grad(self.handle, nx, ny, nz, nb, _p(rhs), _p(prev), _p(target), _p(mask),
+        _check(_sig().bbpp_net_loss_grad(self.handle, nx, ny, nz, nb, h2, _p(r), _p(prev), _p(target), _p(mask),
                                          ctypes.byref(loss), None if g is None else g.ctypes.data))
         return loss.value, g
 
     def train(self, data, steps, batch=4, lr=2e-3, seed=7):
         nx, ny, nz = data.dims
         hist = np.zeros(max(steps, 1), np.float32)
-        _check(_sig().bbpp_net_train(self.handle, nx, ny, nz, data.n, data.rhs.ptr, data.prev.ptr, data.target.ptr,
-                                     _p(data.mask), steps, batch, lr, seed, hist.ctypes.data))
+        _check(_sig().bbpp_net_train(self.handle, nx, ny, nz, data.n, data.h2, data.r.ptr, data.prev.ptr,
+                                     data.target.ptr, _p(data.mask), steps, batch, lr, seed, hist.ctypes.data))
         return hist[:steps]
 
-    def infer(self, dims, rhs, prev, mask, out):
+    def infer(self, dims, h2, r, prev, mask, out):
         nx, ny, nz = dims
-        _check(_sig().bbpp_net_infer(self.handle, nx, ny, nz, _p(rhs), _p(prev), _p(mask), _p(out)))
+        _check(_sig().bbpp_net_infer(self.handle, nx, ny, nz, h2, _p(r), _p(prev), _p(mask), _p(out)))
 
     def save(self, path):
         _check(_sig().bbpp_net_save(self.handle, path.encode()))
@@ -111,11 +112,12 @@ class Net:
 
 
 class OUData:
-    """Device-resident training triples (FP32): rhs_t, p_{t-1}, p_t."""
+    """Device-resident training samples (FP32): the residual r_t of the warm
+    start p_{t-1} for rhs_t, p_{t-1}, and the correction p_t - p_{t-1}."""
 
-    def __init__(self, dims, mask, rhs, prev, target, seconds):
-        self.dims, self.mask, self.rhs, self.prev, self.target = dims, mask, rhs, prev, target
-        self.n = rhs.shape[0]
+    def __init__(self, dims, h2, mask, r, prev, target, seconds):
+        self.dims, self.h2, self.mask, self.r, self.prev, self.target = dims, h2, mask, r, prev, target
+        self.n = r.shape[0]
         self.gen_seconds = seconds
 
 
@@ -144,19 +146,23 @@ def make_ou_dataset(n, nsamples, nsph, rad, seed, tol=1e-10, bc="ppn"):
     dm = DeviceArray(g.shape, np.uint8)
     s.sphere_mask(cents, radii, dm)
     mh = dm.download()
-    rhs = np.zeros((nsamples,) + g.shape, np.float32)
-    prev = np.zeros_like(rhs)
-    tgt = np.zeros_like(rhs)
+    res = np.zeros((nsamples,) + g.shape, np.float32)
+    prev = np.zeros_like(res)
+    tgt = np.zeros_like(res)
+    db, dp, dr = (DeviceArray(g.shape, np.float64) for _ in range(3))
     last = None
     k = 0
-    for r, p, rep in ou_sequence_solves(g, dm, mh, nsamples + 1, seed, tol):
+    for rhs, p, rep in ou_sequence_solves(g, dm, mh, nsamples + 1, seed, tol):
         if last is not None and k < nsamples:
-            rhs[k] = r
+            db.upload(rhs)
+            dp.upload(last)
+            s.residual(db, dp, dr, dm)
+            res[k] = dr.download()
             prev[k] = last
-            tgt[k] = p
+            tgt[k] = p - last
             k += 1
         last = p
-    data = OUData(g.shape[::-1], dm, DeviceArray.from_host(rhs), DeviceArray.from_host(prev),
+    data = OUData(g.shape[::-1], g.dx * g.dy, dm, DeviceArray.from_host(res), DeviceArray.from_host(prev),
                   DeviceArray.from_host(tgt), time.time() - t0)
     return data, g, (cents, radii)
 

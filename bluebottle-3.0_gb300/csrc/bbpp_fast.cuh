@@ -527,6 +527,121 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
   }
 }
 
+
+// ------------------------------------------------------- K1, cached ---
+// FP32 search kernel without shared-memory staging: each thread forms p_new
+// for its pair of x-adjacent cells and their six neighbours straight from the
+// read-only cache (the FP32 FMAs are cheap, so recomputing a neighbour's p_new
+// costs nothing the memory system notices), then Ap and (p, Ap).  Blocks are
+// 64 x 8 cells of one plane, so y neighbours hit L1 and z neighbours L2; DRAM
+// sees each array about once.  No barriers, no halo bookkeeping.
+template <bool MASK, bool ISO>
+__global__ void __launch_bounds__(FNT) k1_cached(const GeoL G, const float *__restrict__ r,
+                                                 const float *__restrict__ pold, float *__restrict__ pnew,
+                                                 float *__restrict__ Ap, const uint8_t *__restrict__ mask,
+                                                 DevState *st, double *partials) {
+  __shared__ float s_dL[27], s_inv[27];
+  __shared__ double s_red[FNT / 32];
+  if (*(volatile int *)&st->done) return;
+  const bool first = *(volatile int *)&st->first;
+  const float beta = first ? 0.f : (float)(*(volatile double *)&st->beta);
+  load_tabs<float>(G, s_dL, s_inv);
+  __syncthreads();
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int gx = blockIdx.x * 64 + 2 * tx, gy = blockIdx.y * 8 + ty, gz = blockIdx.z;
+  float acc = 0.f;
+  if (gx < nx && gy < ny) {
+    const unsigned int plane = (unsigned int)nx * ny;
+    const unsigned int c = plane * gz + (unsigned int)nx * gy + gx;
+    const bool two = gx + 1 < nx;
+    const int wxa = wall_count(gx, nx, G.px), wxb = two ? wall_count(gx + 1, nx, G.px) : 0;
+    const int wyz = 3 * wall_count(gy, ny, G.py) + 9 * wall_count(gz, nz, G.pz);
+    const bool interior = wxa + wxb + wyz == 0;
+    // p_new of a cell from its (r, p_old) and wall class
+    auto pn = [&](unsigned int q, int cls) -> float {
+      float rv = __ldg(r + q);
+      if (cls) rv *= s_inv[cls];
+      return first ? rv : fmaf(beta, __ldg(pold + q), rv);
+    };
+    auto pn2 = [&](unsigned int q, int cla, int clb, float &a, float &b) {
+      if (two && !(q & 1u)) {
+        const float2 rv = __ldg(reinterpret_cast<const float2 *>(r + q));
+        float2 pv = make_float2(0.f, 0.f);
+        if (!first) pv = __ldg(reinterpret_cast<const float2 *>(pold + q));
+        const float ra = cla ? rv.x * s_inv[cla] : rv.x, rb = clb ? rv.y * s_inv[clb] : rv.y;
+        a = fmaf(beta, pv.x, ra);
+        b = fmaf(beta, pv.y, rb);
+      } else {
+        a = pn(q, cla);
+        b = two ? pn(q + 1, clb) : 0.f;
+      }
+    };
+    float c0, c1;
+    pn2(c, wxa + wyz, wxb + wyz, c0, c1);
+    // x neighbours
+    const int xw = halo_index(gx - 1, nx, G.px), xe = halo_index(gx + (two ? 2 : 1), nx, G.px);
+    const unsigned int row = plane * gz + (unsigned int)nx * gy;
+    const float pw = xw >= 0 ? pn(row + xw, wall_count(xw, nx, G.px) + wyz) : 0.f;
+    const float pe = xe >= 0 ? pn(row + xe, wall_count(xe, nx, G.px) + wyz) : 0.f;
+    // y and z neighbours (pairs at the same x)
+    float n0 = 0.f, n1 = 0.f, s0 = 0.f, s1 = 0.f, t0 = 0.f, t1 = 0.f, b0 = 0.f, b1 = 0.f;
+    const int yn = halo_index(gy + 1, ny, G.py), ys = halo_index(gy - 1, ny, G.py);
+    const int zt = halo_index(gz + 1, nz, G.pz), zb = halo_index(gz - 1, nz, G.pz);
+    const int wz = 9 * wall_count(gz, nz, G.pz);
+    if (yn >= 0) {
+      const int cy = 3 * wall_count(yn, ny, G.py) + wz;
+      pn2(plane * gz + (unsigned int)nx * yn + gx, wxa + cy, wxb + cy, n0, n1);
+    }
+    if (ys >= 0) {
+      const int cy = 3 * wall_count(ys, ny, G.py) + wz;
+      pn2(plane * gz + (unsigned int)nx * ys + gx, wxa + cy, wxb + cy, s0, s1);
+    }
+    const int wy = 3 * wall_count(gy, ny, G.py);
+    if (zt >= 0) {
+      const int cz = wy + 9 * wall_count(zt, nz, G.pz);
+      pn2(plane * zt + (unsigned int)nx * gy + gx, wxa + cz, wxb + cz, t0, t1);
+    }
+    if (zb >= 0) {
+      const int cz = wy + 9 * wall_count(zb, nz, G.pz);
+      pn2(plane * zb + (unsigned int)nx * gy + gx, wxa + cz, wxb + cz, b0, b1);
+    }
+    float a0, a1;
+    if (interior) {
+      a0 = apply_L<float, ISO>(G, s_dL, 0, c0, two ? c1 : pe, pw, n0, s0, t0, b0);
+      a1 = apply_L<float, ISO>(G, s_dL, 0, c1, pe, c0, n1, s1, t1, b1);
+    } else {
+      a0 = apply_L<float, ISO>(G, s_dL, wxa + wyz, c0, two ? c1 : pe, pw, n0, s0, t0, b0);
+      a1 = apply_L<float, ISO>(G, s_dL, wxb + wyz, c1, pe, c0, n1, s1, t1, b1);
+    }
+    if (MASK) {
+      if (mask[c]) a0 = 0.f;
+      if (two && mask[c + 1]) a1 = 0.f;
+    }
+    if (two && !(c & 1u)) {
+      *reinterpret_cast<float2 *>(pnew + c) = make_float2(c0, c1);
+      *reinterpret_cast<float2 *>(Ap + c) = make_float2(a0, a1);
+    } else {
+      pnew[c] = c0;
+      Ap[c] = a0;
+      if (two) {
+        pnew[c + 1] = c1;
+        Ap[c + 1] = a1;
+      }
+    }
+    acc = fmaf(c0, a0, acc);
+    if (two) acc = fmaf(c1, a1, acc);
+  }
+  double v[1] = {(double)acc}, tot[1];
+  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && threadIdx.x == 0) {
+    st->pAp = tot[0];
+    st->alpha = st->rz / tot[0];
+    st->first = 0;
+  }
+}
+
 // ------------------------------------------------------------------ K2 ----
 template <typename T> struct Vec2;
 template <> struct Vec2<double> { typedef double2 type; };

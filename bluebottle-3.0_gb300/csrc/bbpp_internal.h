@@ -56,6 +56,7 @@ struct bbpp_ctx {
   int fkz = 1;         // z planes per CTA of the residual kernel
   dim3 fgrid;          // grid of the residual kernel (32x16 tiles)
   int pkz[2] = {1, 1};  // z planes per CTA of the search kernel [FP32, FP64]
+  bool fp32_cached = true;  // FP32 search kernel: cache-fed (true) or z-marching
   dim3 pgrid[2];        // grid of the search kernel (64x16 tiles) [FP32, FP64]
   int egrid = 1;       // elementwise grid (1-D)
   size_t nparts = 0;   // capacity of partials (per sum)
@@ -103,6 +104,8 @@ void bbpp_launch_resid_s(bbpp_ctx *ctx, const uint8_t *mask, TXT *x, const TXT *
 int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o, bool zero_x,
                   bbpp_report *rep);
 void bbpp_ir_free(bbpp_ctx *ctx);
+
+int bbpp_residual_async(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x, double *r);
 
 // learned initial guess (bbpp_net.cu)
 int bbpp_net_guess(bbpp_ctx *ctx, void *net, const uint8_t *mask, const double *rhs, const double *prev, double *x,

@@ -2,8 +2,15 @@
 // on BF16 tensor cores, trained on the GPU with the library's own forward and
 // backward kernels (bbpp_conv.cuh), and applied before the PCG.
 //
+// The network predicts the correction to a warm start: with p_prev the
+// previous pressure and r = rhs - (-A) p_prev its residual (both computed from
+// the inputs the guess is defined on: rhs, p_prev, mask),
+//   p0 = p_prev + h^2 s_r^-1 OUT,    OUT ~ net(r / s_r, p_prev / s_p, mask)
+// so that in grid units OUT approximates the unit-spacing inverse Laplacian of
+// the normalised residual, a local relation that carries over between grid
+// resolutions.  s_r, s_p: fluid RMS of r and p_prev.
 // Network (channels-last BF16 activations, FP32 master weights, Adam):
-//   X0  [V][16]  = (rhs / s_b, prev / s_p, mask, 0 ...)      s_* = fluid RMS
+//   X0  [V][16]  = (r / s_r, prev / s_p, mask, 0 ...)
 //   E1  = relu(conv3(X0;  16 -> 16))      stored in CAT1[:, 32:48]
 //   P1  = avgpool2(E1)                    [V/8][16]
 //   E2  = relu(conv3(P1;  16 -> 32))      stored in CAT2[:, 64:96]
@@ -11,8 +18,8 @@
 //   E3  = relu(conv3(P2;  32 -> 64))      [V/64][64]
 //   CAT2[:, 0:64] = up2(E3);  D2 = relu(conv3(CAT2; 96 -> 32))   [V/8][32]
 //   CAT1[:, 0:32] = up2(D2);  D1 = relu(conv3(CAT1; 48 -> 16))   [V][16]
-//   OUT = D1 . w_head + b_head  (FP32)    p0 = s_p OUT on fluid cells, 0 on solid
-// Loss: mean over fluid cells of (OUT - p*/s_p)^2.
+//   OUT = D1 . w_head + b_head  (FP32)
+// Loss: mean over fluid cells of (OUT - (p* - p_prev) s_r / h^2)^2.
 // Padding is periodic in x and y and zero in z (the workloads' boundaries).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -332,11 +339,12 @@ __global__ void k_head_bwd(const float *__restrict__ dout, const bf16 *__restric
   }
 }
 
-// loss = sum over volumes and fluid cells of (OUT - tgt s_p)^2 / nfluid_total;
-// dOUT = 2 (OUT - tgt s_p) / nfluid_total on fluid cells, 0 on solid cells
+// loss = sum over volumes and fluid cells of (OUT - tgt / (s_r h^2))^2 / nfluid_total
+// with tgt = p* - p_prev;  dOUT = 2 (OUT - tgt / (s_r h^2)) / nfluid_total on
+// fluid cells, 0 on solid cells
 __global__ void k_loss(const float *__restrict__ out, const float *__restrict__ tgt, const uint8_t *__restrict__ mask,
-                       const float *__restrict__ scales, long long vol, int nb, double inv_n, float *__restrict__ dout,
-                       double *loss) {
+                       const float *__restrict__ scales, long long vol, int nb, double inv_n, float inv_h2,
+                       float *__restrict__ dout, double *loss) {
   __shared__ double s[256];
   double a = 0;
   const long long n = vol * nb;
@@ -347,7 +355,7 @@ __global__ void k_loss(const float *__restrict__ out, const float *__restrict__ 
       dout[e] = 0.f;
       continue;
     }
-    const float d = out[e] - tgt[e] * scales[2 * b + 1];
+    const float d = out[e] - tgt[e] * (scales[2 * b] * inv_h2);
     a += (double)d * d;
     dout[e] = (float)(2.0 * inv_n) * d;
   }
@@ -360,12 +368,13 @@ __global__ void k_loss(const float *__restrict__ out, const float *__restrict__ 
   if (threadIdx.x == 0) atomicAdd(loss, s[0] * inv_n);
 }
 
-// p0 = OUT / (1/s_p) on fluid cells, 0 on solid cells
-__global__ void k_guess_out(const float *__restrict__ out, const uint8_t *__restrict__ mask,
-                            const float *__restrict__ scales, long long vol, double *__restrict__ x) {
-  const double sp = 1.0 / (double)scales[1];
+// p0 = p_prev + OUT h^2 / (1/s_r) on fluid cells, 0 on solid cells
+__global__ void k_guess_out(const float *__restrict__ out, const double *__restrict__ prev,
+                            const uint8_t *__restrict__ mask, const float *__restrict__ scales, double h2,
+                            long long vol, double *__restrict__ x) {
+  const double sr = h2 / (double)scales[0];
   for (long long i = blockIdx.x * 256LL + threadIdx.x; i < vol; i += (long long)gridDim.x * 256)
-    x[i] = (mask && mask[i]) ? 0.0 : (double)out[i] * sp;
+    x[i] = (mask && mask[i]) ? 0.0 : (prev ? prev[i] : 0.0) + (double)out[i] * sr;
 }
 
 __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
@@ -414,6 +423,7 @@ struct bbpp_net {
   bf16 *dD1 = nullptr, *G = nullptr, *dCAT1 = nullptr, *dD2 = nullptr, *dCAT2 = nullptr, *dE3 = nullptr,
        *dP2 = nullptr, *dE2 = nullptr, *dP1 = nullptr, *dE1 = nullptr;
   cudaStream_t stream = nullptr;
+  long long launches = 0;  // kernels launched by inference / training
 };
 
 static void free_work(bbpp_net *n) {
@@ -553,6 +563,7 @@ static int forward(bbpp_net *n, int nx, int ny, int nz, int nb) {
   e = conv_fwd(48, 16, cargs(n, nx, ny, nz, nb, n->CAT1, 48, 0, W + L[4].woff, Bf + L[4].boff, n->D1, 16, 0, 1), s);
   if (e != cudaSuccess) return BBPP_CUDA_ERROR;
   k_head_fwd<<<nblocks(V), 256, 0, s>>>(n->D1, n->w + n->head_w, n->w + n->head_b, V, n->OUT);
+  n->launches += 10;
   NCK(cudaGetLastError());
   return 0;
 }
@@ -621,6 +632,7 @@ static int prepare(bbpp_net *n, int nx, int ny, int nz, int nb, const T *rhs, co
   if (prev) k_fluid_sumsq<T><<<g, 256, 0, s>>>(prev, mask, vol, nb, n->sums + 2 * nb);
   k_scales<<<1, 256, 0, s>>>(n->sums, prev ? n->sums + 2 * nb : nullptr, nb, n->scales);
   k_prep<T><<<nblocks(vol * nb), 256, 0, s>>>(rhs, prev, mask, n->scales, vol, nb, n->X0);
+  n->launches += prev ? 4 : 3;
   NCK(cudaGetLastError());
   return 0;
 }
@@ -725,9 +737,11 @@ extern "C" int bbpp_net_set_params(bbpp_net *n, const float *host) {
 
 // Forward (FP32 inputs), loss and gradients: loss to *loss, gradients to grads
 // (host, np floats) when not null.  Volumes of nx*ny*nz stacked nb times;
-// mask (one volume) may be null.
-extern "C" int bbpp_net_loss_grad(bbpp_net *n, int nx, int ny, int nz, int nb, const float *rhs, const float *prev,
-                                  const float *target, const uint8_t *mask, double *loss, float *grads) {
+// mask (one volume) may be null.  rhs holds the residual r of p_prev, target
+// the correction p* - p_prev; h2 is the squared grid spacing.
+extern "C" int bbpp_net_loss_grad(bbpp_net *n, int nx, int ny, int nz, int nb, double h2, const float *rhs,
+                                  const float *prev, const float *target, const uint8_t *mask, double *loss,
+                                  float *grads) {
   if (!n || !rhs || !target || nb < 1) return BBPP_BAD_ARG;
   int rc = check_dims(nx, ny, nz);
   if (rc) return rc;
@@ -749,8 +763,8 @@ extern "C" int bbpp_net_loss_grad(bbpp_net *n, int nx, int ny, int nz, int nb, c
   }
   const double inv_n = 1.0 / std::max<long long>(1, nfl * nb);
   NCK(cudaMemsetAsync(n->lossd, 0, sizeof(double), s));
-  k_loss<<<std::min(nblocks(vol * nb), 1024), 256, 0, s>>>(n->OUT, target, mask, n->scales, vol, nb, inv_n, n->dOUT,
-                                                            n->lossd);
+  k_loss<<<std::min(nblocks(vol * nb), 1024), 256, 0, s>>>(n->OUT, target, mask, n->scales, vol, nb, inv_n,
+                                                            (float)(1.0 / h2), n->dOUT, n->lossd);
   NCK(cudaMemsetAsync(n->g, 0, n->np * sizeof(float), s));
   rc = backward(n, nx, ny, nz, nb);
   if (rc) return rc;
@@ -763,9 +777,9 @@ extern "C" int bbpp_net_loss_grad(bbpp_net *n, int nx, int ny, int nz, int nb, c
 // Train on a device-resident set of nsamples volumes (FP32 rhs, prev, target;
 // one shared mask): `steps` Adam steps on batches of `batch` volumes drawn
 // with Ranq1.  loss_hist (host, steps) may be null.
-extern "C" int bbpp_net_train(bbpp_net *n, int nx, int ny, int nz, int nsamples, const float *rhs, const float *prev,
-                              const float *target, const uint8_t *mask, int steps, int batch, float lr,
-                              unsigned long long seed, float *loss_hist) {
+extern "C" int bbpp_net_train(bbpp_net *n, int nx, int ny, int nz, int nsamples, double h2, const float *rhs,
+                              const float *prev, const float *target, const uint8_t *mask, int steps, int batch,
+                              float lr, unsigned long long seed, float *loss_hist) {
   if (!n || !rhs || !target || nsamples < 1 || batch < 1 || steps < 0) return BBPP_BAD_ARG;
   int rc = check_dims(nx, ny, nz);
   if (rc) return rc;
@@ -788,7 +802,7 @@ extern "C" int bbpp_net_train(bbpp_net *n, int nx, int ny, int nz, int nsamples,
                           n->stream));
     }
     double loss = 0;
-    rc = bbpp_net_loss_grad(n, nx, ny, nz, batch, brhs, prev ? bprev : nullptr, btgt, mask, &loss, nullptr);
+    rc = bbpp_net_loss_grad(n, nx, ny, nz, batch, h2, brhs, prev ? bprev : nullptr, btgt, mask, &loss, nullptr);
     if (rc) break;
     n->t++;
     const float c1 = 1.f / (1.f - powf(b1, (float)n->t)), c2 = 1.f / (1.f - powf(b2, (float)n->t));
@@ -806,10 +820,10 @@ extern "C" int bbpp_net_train(bbpp_net *n, int nx, int ny, int nz, int nsamples,
   return rc;
 }
 
-// Inference for one volume (FP64 rhs / prev as the solver holds them) into
-// p0 (FP64): p0 = s_p OUT on fluid cells, 0 on solid cells.
-extern "C" int bbpp_net_infer(bbpp_net *n, int nx, int ny, int nz, const double *rhs, const double *prev,
-                              const uint8_t *mask, double *p0) {
+// Inference for one volume (FP64 r = rhs - (-A) p_prev and p_prev, as the
+// solver holds them) into p0 = p_prev + h2 OUT / (1/s_r) (FP64), 0 on solid cells.
+extern "C" int bbpp_net_infer(bbpp_net *n, int nx, int ny, int nz, double h2, const double *rhs,
+                              const double *prev, const uint8_t *mask, double *p0) {
   if (!n || !rhs || !p0) return BBPP_BAD_ARG;
   int rc = check_dims(nx, ny, nz);
   if (rc) return rc;
@@ -820,7 +834,8 @@ extern "C" int bbpp_net_infer(bbpp_net *n, int nx, int ny, int nz, const double 
   rc = forward(n, nx, ny, nz, 1);
   if (rc) return rc;
   const long long vol = (long long)nx * ny * nz;
-  k_guess_out<<<nblocks(vol), 256, 0, n->stream>>>(n->OUT, mask, n->scales, vol, p0);
+  k_guess_out<<<nblocks(vol), 256, 0, n->stream>>>(n->OUT, prev, mask, n->scales, h2, vol, p0);
+  n->launches += 1;
   NCK(cudaGetLastError());
   return 0;
 }
@@ -931,7 +946,17 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
   cudaStream_t saved = n->stream;
   n->stream = ctx->stream;
   cudaEventRecord(e0, ctx->stream);
-  int rc = bbpp_net_infer(n, ctx->G.nx, ctx->G.ny, ctx->G.nz, rhs, prev, mask, x);
+  // residual of the warm start into the solver's free Ap buffer
+  const double *r = rhs;
+  int rc = 0;
+  if (prev) {
+    rc = bbpp_residual_async(ctx, mask, rhs, prev, ctx->Ap);
+    r = ctx->Ap;
+  }
+  const double h2 = ctx->grid.dx * ctx->grid.dy;
+  const long long l0 = n->launches;
+  if (rc == 0) rc = bbpp_net_infer(n, ctx->G.nx, ctx->G.ny, ctx->G.nz, h2, r, prev, mask, x);
+  ctx->launches += (n->launches - l0) + (prev ? 1 : 0);
   cudaEventRecord(e1, ctx->stream);
   n->stream = saved;
   if (rc == 0) {

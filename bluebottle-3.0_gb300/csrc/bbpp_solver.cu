@@ -259,13 +259,18 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
   ctx->grid = *g;
   geol_init(ctx->G, &ctx->GL);
   ctx->sms = dev_sms();
+  {
+    const char *e = getenv("BBPP_FP32_SEARCH");  // "marched" selects the z-marching FP32 kernel
+    ctx->fp32_cached = !(e && strcmp(e, "marched") == 0);
+  }
   stencil_shape(ctx);
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
       std::max<size_t>(std::max<size_t>((size_t)ctx->sgrid.x * ctx->sgrid.y * ctx->sgrid.z, (size_t)ctx->egrid),
                        (size_t)ctx->fgrid.x * ctx->fgrid.y * ctx->fgrid.z),
-      std::max<size_t>((size_t)ctx->pgrid[0].x * ctx->pgrid[0].y * ctx->pgrid[0].z,
-                       (size_t)ctx->pgrid[1].x * ctx->pgrid[1].y * ctx->pgrid[1].z));
+      std::max<size_t>(std::max<size_t>((size_t)ctx->pgrid[0].x * ctx->pgrid[0].y * ctx->pgrid[0].z,
+                                        (size_t)ctx->pgrid[1].x * ctx->pgrid[1].y * ctx->pgrid[1].z),
+                       (size_t)((ctx->G.nx + 63) / 64) * ((ctx->G.ny + 7) / 8) * ctx->G.nz));
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   ctx->stream = ctx->own_stream;
@@ -371,25 +376,42 @@ extern "C" const char *bbpp_version(void) { return "bbpp 0.1 (sm_103a)"; }
 
 // ---------------------------------------------------------------- launches --
 // All launches go to ctx->stream.  Typed on the vector element.
+static void launch_search_cached(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const float *pold,
+                                 float *pnew, float *Ap, DevState *st) {
+  const dim3 g((ctx->G.nx + 63) / 64, (ctx->G.ny + 7) / 8, ctx->G.nz);
+  cudaStream_t s = ctx->stream;
+  if (mask) {
+    if (ctx->GL.iso) k1_cached<true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
+    else k1_cached<true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
+  } else {
+    if (ctx->GL.iso) k1_cached<false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
+    else k1_cached<false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
+  }
+}
+
 template <typename T>
 static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap,
                                DevState *st) {
   // bytes/cell: read r, p_old (+ mask), write p_new, Ap
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_SEARCH_SPMV : KK_SEARCH_SPMV_F32, 4.0 * sizeof(T) + (mask ? 1 : 0));
   const int prec = sizeof(T) == 8 ? 1 : 0;
-  const dim3 g = ctx->pgrid[prec];
-  const int kz = ctx->pkz[prec];
   cudaStream_t s = ctx->stream;
-  if (mask) {
-    if (ctx->GL.iso)
-      k1_search2<T, true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
-    else
-      k1_search2<T, true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+  if (prec == 0 && ctx->fp32_cached) {
+    launch_search_cached(ctx, mask, (const float *)r, (const float *)pold, (float *)pnew, (float *)Ap, st);
   } else {
-    if (ctx->GL.iso)
-      k1_search2<T, false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
-    else
-      k1_search2<T, false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+    const dim3 g = ctx->pgrid[prec];
+    const int kz = ctx->pkz[prec];
+    if (mask) {
+      if (ctx->GL.iso)
+        k1_search2<T, true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+      else
+        k1_search2<T, true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+    } else {
+      if (ctx->GL.iso)
+        k1_search2<T, false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+      else
+        k1_search2<T, false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+    }
   }
   bbpp_rec_end(ctx);
 }
@@ -783,6 +805,17 @@ extern "C" int bbpp_residual(bbpp_ctx *ctx, const uint8_t *mask, const double *r
   CK(cudaStreamSynchronize(ctx->stream));
   if (rr) *rr = hst->rr;
   if (bb) *bb = hst->bb;
+  return 0;
+}
+
+// r = rhs - (-A) x on the context's stream, no synchronisation (internal)
+int bbpp_residual_async(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x, double *r) {
+  DevState *st = ctx->st + 1, *hst = ctx->hst + 1;
+  memset(hst, 0, sizeof(DevState));
+  hst->stop = 1;
+  CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+  launch_resid<double, double>(ctx, mask, x, rhs, r, st, RES_INIT);
+  CK(cudaGetLastError());
   return 0;
 }
 

@@ -188,16 +188,20 @@ int bbpp_net_destroy(bbpp_net *net);
 int bbpp_net_num_params(const bbpp_net *net);
 int bbpp_net_get_params(const bbpp_net *net, float *host);
 int bbpp_net_set_params(bbpp_net *net, const float *host);
-/* Loss (mean over fluid cells of (out - target/s_p)^2) and its gradient
- * (host array of num_params floats, may be NULL) for nb stacked volumes. */
-int bbpp_net_loss_grad(bbpp_net *net, int nx, int ny, int nz, int nb, const float *rhs, const float *prev,
-                       const float *target, const uint8_t *mask, double *loss, float *grads_host);
+/* The network predicts the correction to the previous pressure p_prev from
+ * r = rhs - (-A) p_prev, p_prev and the mask: p0 = p_prev + h2 out / (1/s_r),
+ * s_r the fluid RMS of r.  Loss: mean over fluid cells of
+ * (out - target / (s_r h2))^2 with target = p* - p_prev; gradient to a host
+ * array of num_params floats (may be NULL) for nb stacked volumes. */
+int bbpp_net_loss_grad(bbpp_net *net, int nx, int ny, int nz, int nb, double h2, const float *r,
+                       const float *prev, const float *target, const uint8_t *mask, double *loss,
+                       float *grads_host);
 /* Adam training on nsamples device-resident volumes (batches drawn by Ranq1). */
-int bbpp_net_train(bbpp_net *net, int nx, int ny, int nz, int nsamples, const float *rhs, const float *prev,
-                   const float *target, const uint8_t *mask, int steps, int batch, float lr,
-                   unsigned long long seed, float *loss_hist_host);
-/* p0 (FP64) from rhs and prev (FP64, prev may be NULL) for one volume. */
-int bbpp_net_infer(bbpp_net *net, int nx, int ny, int nz, const double *rhs, const double *prev,
+int bbpp_net_train(bbpp_net *net, int nx, int ny, int nz, int nsamples, double h2, const float *r,
+                   const float *prev, const float *target, const uint8_t *mask, int steps, int batch,
+                   float lr, unsigned long long seed, float *loss_hist_host);
+/* p0 (FP64) from r and p_prev (FP64, p_prev may be NULL: then r = rhs). */
+int bbpp_net_infer(bbpp_net *net, int nx, int ny, int nz, double h2, const double *r, const double *prev,
                    const uint8_t *mask, double *p0);
 int bbpp_net_set_stream(bbpp_net *net, void *stream);
 int bbpp_net_save(const bbpp_net *net, const char *path);

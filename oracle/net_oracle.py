@@ -51,15 +51,16 @@ def up(x):
     return F.interpolate(x, scale_factor=2, mode="nearest")
 
 
-def loss_and_grad(params, rhs, prev, target, mask):
-    """Loss and its gradient with respect to the flat parameter vector."""
+def loss_and_grad(params, r, prev, target, mask, h2):
+    """Loss and its gradient with respect to the flat parameter vector; r is
+    the residual of the warm start prev, target the correction p* - prev."""
     w = torch.tensor(np.asarray(params, dtype=np.float32), requires_grad=True)
-    L = loss_torch(w, rhs, prev, target, mask)
+    L = loss_torch(w, r, prev, target, mask, h2)
     L.backward()
-    return float(L), w.grad.numpy().copy()
+    return float(L.detach()), w.grad.numpy().copy()
 
 
-def loss_torch(w, rhs, prev, target, mask):
+def loss_torch(w, rhs, prev, target, mask, h2):
     """Loss of the network with parameters w (torch tensor, differentiable)."""
     off = 0
     layers = []
@@ -102,5 +103,5 @@ def loss_torch(w, rhs, prev, target, mask):
     cat1 = torch.cat([up(d2), e1], dim=1)
     d1 = conv3(cat1, w5, b5, relu=True)
     out = torch.einsum("nczyx,c->nzyx", d1, hw) + hb
-    d = (out - target * sc[:, 1].view(-1, 1, 1, 1))[:, fluid]
+    d = (out - target * (sc[:, 0] / h2).view(-1, 1, 1, 1))[:, fluid]
     return (d * d).sum() / d.numel()

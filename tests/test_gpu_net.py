@@ -90,9 +90,9 @@ def test_conv3_forward_dgrad_wgrad(bbpp_lib, cin, cout, dims, pads):
 def _small_problem(seed, dims=(16, 16, 8), nb=2):
     nx, ny, nz = dims
     rng = np.random.default_rng(seed)
-    rhs = rng.normal(size=(nb, nz, ny, nx)).astype(np.float32)
+    rhs = rng.normal(size=(nb, nz, ny, nx)).astype(np.float32)  # residual of the warm start
     prev = rng.normal(size=(nb, nz, ny, nx)).astype(np.float32)
-    tgt = (0.7 * prev + 0.1 * rng.normal(size=(nb, nz, ny, nx))).astype(np.float32)
+    tgt = (0.01 * rhs + 0.001 * rng.normal(size=(nb, nz, ny, nx))).astype(np.float32)  # correction
     mask = (rng.random((nz, ny, nx)) < 0.05).astype(np.uint8)
     return rhs, prev, tgt, mask
 
@@ -103,8 +103,9 @@ def test_net_gradient_matches_cpu_reference(bbpp_lib):
     rhs, prev, tgt, mask = _small_problem(1)
     dims = (16, 16, 8)
     d = [bbpp.DeviceArray.from_host(a) for a in (rhs, prev, tgt, mask)]
-    loss, g = net.loss_grad(dims, d[0], d[1], d[2], d[3])
-    Lr, gr = NO.loss_and_grad(p, torch.as_tensor(rhs), torch.as_tensor(prev), torch.as_tensor(tgt), mask)
+    h2 = 1.0 / 256.0
+    loss, g = net.loss_grad(dims, h2, d[0], d[1], d[2], d[3])
+    Lr, gr = NO.loss_and_grad(p, torch.as_tensor(rhs), torch.as_tensor(prev), torch.as_tensor(tgt), mask, h2)
     assert abs(loss - Lr) <= 2e-2 * Lr
     cos = float(g @ gr / (np.linalg.norm(g) * np.linalg.norm(gr)))
     assert cos > 0.99, cos

@@ -172,3 +172,25 @@ def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol):
     err = np.abs(x - xo).max() / np.abs(xo).max()
     # the solution error is bounded by the residual times the condition number
     assert err < 1e4 * tol, err
+
+
+@pytest.mark.parametrize("dims,bc", SHAPES)
+@pytest.mark.parametrize("precision", [bbpp.FP64, bbpp.FP32_IR])
+def test_solve_odd_shapes(lib, orc, dims, bc, precision):
+    """Whole solves on odd, tile-edge and tiny grids with every boundary mix,
+    masked, through both search kernels (FP64 z-marching, FP32 cache-fed)."""
+    nx, ny, nz = dims
+    g = bbpp.Grid.make(nx, ny, nz, 1.0 / nx, 1.0 / ny, 1.0 / nz, bc)
+    mask = rand_mask(g.shape, nx + ny, 0.1)
+    rng = np.random.default_rng(nx * ny)
+    b = rng.uniform(-1, 1, g.shape)
+    b[mask == 1] = 0
+    b[mask == 0] -= b[mask == 0].mean()
+    s = bbpp.Solver(g)
+    tol = 1e-10 if precision == bbpp.FP64 else 1e-8
+    x, rep = s.solve_host(b, mask, tol=tol, precision=precision)
+    assert rep.status == bbpp.CONVERGED and rep.true_rel <= tol * 1.01
+    xo, res = orc.pcg(to_orc(orc, g), b, mask, tol=1e-13)
+    assert np.all(x[mask == 1] == 0)
+    err = np.abs(x - xo).max() / max(np.abs(xo).max(), 1e-300)
+    assert err < 1e4 * tol, err
