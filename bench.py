@@ -30,7 +30,7 @@ WORKLOAD = ("C3: 256^3 cells, periodic x/y + Neumann z, 1000 spheres r=6 cells, 
 # Plain FP64 PCG iterations of the C3 workload to 1e-8 (seed 3), measured by
 # the CUDA path and equal to the oracle's count; used to scale the bounded CPU
 # sample of the reference arm to a full solve.
-C3_FP64_ITERS = None  # filled from the GPU run when available; see cpu_iters()
+C3_FP64_ITERS = 604
 
 
 def peaks():
@@ -145,6 +145,17 @@ def train_c4_net(args):
     return net, info
 
 
+def profiler_api():
+    """cuProfilerStart/Stop of the driver for the current context (a no-op
+    where the driver library is missing)."""
+    import ctypes
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+    except OSError:
+        return lambda on: None
+    return lambda on: (cu.cuProfilerStart() if on else cu.cuProfilerStop())
+
+
 def cpu_sample(g, rhs, mask, iters_full, threads):
     """Time the oracle PCG on the full-size workload for a bounded number of
     iterations and scale to a full solve: t = t_setup + t_iter * iters_full."""
@@ -225,9 +236,10 @@ def run_ours(args):
     net = None
     net_info = None
     methods = {"fp64": dict(precision=bbpp.FP64), "ir": dict(precision=bbpp.FP32_IR),
+               "ir_restart": dict(precision=bbpp.FP32_IR, ir_mode=bbpp.IR_RESTART),
                "ir_warm": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_GIVEN)}
     headline = "ir"
-    if not args.no_learned and not args.only:
+    if not args.no_learned and args.only in (None, "learned_ir"):
         net, net_info = train_c4_net(args)
         methods["learned_ir"] = dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle,
                                      prev=dprev.ptr)
@@ -242,11 +254,17 @@ def run_ours(args):
     prev_host = dprev.download()
 
     if args.only:
-        # solves of one method only (profiler runs): steps solves, no warm-up
+        # solves of one method only (profiler runs): steps solves, no warm-up;
+        # the profiler's collection is switched on around them only
+        # (ncu --profile-from-start off)
+        prof = profiler_api()
+        prof(True)
         for _ in range(args.steps):
             rep = step(methods[args.only])
             assert rep.status == bbpp.CONVERGED
-        print(json.dumps({"only": args.only, "iters": rep.iters, "ms": rep.ms}))
+        bbpp.sync()
+        prof(False)
+        print(json.dumps({"only": args.only, "iters": rep.iters, "ms": rep.ms, "launches": rep.launches}))
         return
 
     for name, kw in methods.items():
@@ -344,8 +362,9 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": H["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32-inner/f64-refined" if headline == "ir" else "f64",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "method": {"ir": "FP32-inner / FP64-refined Jacobi PCG",
-                                                     "learned_ir": "learned guess (C4 net) + FP32-inner / FP64-refined PCG",
+        "config": {"workload": WORKLOAD, "method": {"ir": "FP32 Jacobi PCG with FP64 reliable updates",
+                                                     "learned_ir": "learned guess (C4 net) + FP32 Jacobi PCG with "
+                                                                   "FP64 reliable updates",
                                                      "fp64": "plain FP64 Jacobi PCG"}[headline],
                    "l2": "flushed (512 MB write) before every step; working set 0.9 GB > L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -381,7 +400,7 @@ def main():
     ap.add_argument("--net", default=None, help="load (or save after training) the learned-guess network here")
     ap.add_argument("--train-samples", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=1500)
-    ap.add_argument("--only", default=None, choices=["fp64", "ir"],
+    ap.add_argument("--only", default=None, choices=["fp64", "ir", "ir_restart", "ir_warm", "learned_ir"],
                     help="run only warm-up + steps solves of one method (profiler runs)")
     ap.add_argument("--ref-iters", type=int, default=0,
                     help="iterations of a full solve for the reference arm (0: the measured C3 count)")

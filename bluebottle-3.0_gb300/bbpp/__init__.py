@@ -26,6 +26,7 @@ CONVERGED, TINY_RHS, MAX_ITER, NAN, BAD_ARG, CUDA_ERROR, NO_DEVICE, WAIT_TIMEOUT
 FP64, FP32_IR = 0, 1
 GUESS_ZERO, GUESS_GIVEN, GUESS_LEARNED = 0, 1, 2
 STOP_REF_RZ, STOP_TRUE_REL = 0, 1
+IR_RELIABLE, IR_RESTART = 0, 1
 
 STATUS_NAMES = {0: "converged", 1: "tiny rhs", 2: "max iterations", 3: "nan residual", 4: "bad argument",
                 5: "cuda error", 6: "no device", 7: "device wait timeout"}
@@ -69,7 +70,7 @@ class Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("guess", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("replace_every", ctypes.c_int),
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
-                ("net", ctypes.c_void_p), ("prev", ctypes.c_void_p)]
+                ("net", ctypes.c_void_p), ("prev", ctypes.c_void_p), ("ir_mode", ctypes.c_int)]
 
 
 class Report(ctypes.Structure):

@@ -14,9 +14,9 @@
 // Ap = 0 there.  A fluid cell's solid neighbour then contributes p = 0, which
 // is the reference's dropped off-diagonal (src/solver_kernel.cu:691-707).
 //
-//  k1_search  p = invM r + beta p_old on a 32x16 tile plus halo, ring of three
-//             planes in shared memory, loads of plane z+2 in flight while
-//             plane z is computed; Ap = L p and the (p, Ap) partial.
+//  k1_search2 p = invM r + beta p_old on a 64x16 tile plus halo (two cells per
+//             thread), ring of three planes in shared memory while the CTA
+//             marches in z; Ap = L p and the (p, Ap) partial.
 //  k2_update  x += alpha p, r -= alpha Ap, (r,r) and the wall correction of
 //             (r,z), vector loads.
 //  k_resid_s  r = bscale rhs - L x (solid cells 0) with (r,z), (r,r), (rhs,rhs).
@@ -92,175 +92,13 @@ __device__ __forceinline__ T apply_L(const GeoL &G, const T *s_dL, int cls, T pc
   }
 }
 
-// ------------------------------------------------------------------ K1 ----
-template <typename T, bool MASK, bool ISO>
-__global__ void __launch_bounds__(FNT) k1_search(const GeoL G, const T *__restrict__ r, const T *__restrict__ pold,
-                                                 T *__restrict__ pnew, T *__restrict__ Ap,
-                                                 const uint8_t *__restrict__ mask, DevState *st, double *partials,
-                                                 int kz) {
-  __shared__ T s_dL[27], s_inv[27];
-  __shared__ T sp[3][FHY][FHX];
-  __shared__ uint8_t sm[3][FHY][FHX + 2];
-  __shared__ double s_red[FNT / 32];
-  if (*(volatile int *)&st->done) return;
-  const bool first = *(volatile int *)&st->first;
-  const T beta = first ? T(0) : (T)(*(volatile double *)&st->beta);
-  load_tabs<T>(G, s_dL, s_inv);
-
-  const int tid = threadIdx.x;
-  const int tx = tid & 31, ty = tid >> 5;  // ty in 0..7; rows ty and ty + 8
-  const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY;
-  const int z0 = blockIdx.z * kz, z1 = min(z0 + kz, G.nz);
-  const int nx = G.nx, ny = G.ny, nz = G.nz;
-  const long long sxy = (long long)nx * ny;
-
-  // halo elements owned by this thread: plane-independent part
-  int e_off[FPER];     // gx + nx*gy, or -1 when there is no cell
-  int e_cls[FPER];     // wall class x + 3y part
-  int e_slot[FPER];    // ly * FHX + lx
-  bool e_own[FPER];    // inside the tile (its p_new is written by this CTA)
-#pragma unroll
-  for (int q = 0; q < FPER; q++) {
-    const int e = tid + q * FNT;
-    e_off[q] = -1;
-    e_cls[q] = 0;
-    e_slot[q] = e;
-    e_own[q] = false;
-    if (e < FHE) {
-      const int ly = e / FHX, lx = e - ly * FHX;
-      const int rx = x0 + lx - 1, ry = y0 + ly - 1;
-      const int gx = halo_index(rx, nx, G.px), gy = halo_index(ry, ny, G.py);
-      if (gx >= 0 && gy >= 0) {
-        e_off[q] = gx + nx * gy;
-        e_cls[q] = wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py);
-        e_own[q] = (rx == gx && ry == gy && lx >= 1 && lx <= FX && ly >= 1 && ly <= FY);
-      }
-    }
-  }
-  __syncthreads();
-
-  T vr[FPER], vp[FPER];
-  uint8_t vm[FPER];
-  int cur_gz = -1;
-  auto issue = [&](int zr) {  // global loads of plane zr into registers
-    const int gz = halo_index(zr, nz, G.pz);
-    cur_gz = gz;
-#pragma unroll
-    for (int q = 0; q < FPER; q++) {
-      vr[q] = T(0);
-      vp[q] = T(0);
-      vm[q] = 0;
-      if (gz >= 0 && e_off[q] >= 0) {
-        const long long c = e_off[q] + sxy * gz;
-        vr[q] = r[c];
-        if (!first) vp[q] = pold[c];
-        if (MASK) vm[q] = mask[c];
-      }
-    }
-  };
-  // Walls only in z (periodic x and y): a plane's cells share one wall class,
-  // so interior planes take a path without any per-cell class arithmetic.
-  // (A per-cell branch would be if-converted into predicated FP64
-  // instructions, which still occupy the FP64 pipe.)
-  const bool xy_walls = !(G.px && G.py);
-  auto commit = [&](int slot, int zr) {  // p_new from the registers into the ring
-    const int gz = cur_gz;
-    const int wz = (gz >= 0) ? 9 * wall_count(gz, nz, G.pz) : 0;
-    const bool ownz = (zr >= z0 && zr < z1);
-    if (!xy_walls && wz == 0) {  // interior plane: Jacobi weight 1
-#pragma unroll
-      for (int q = 0; q < FPER; q++) {
-        if (e_slot[q] < FHE) {
-          T val = T(0);
-          if (gz >= 0 && e_off[q] >= 0) {
-            val = first ? vr[q] : fma(beta, vp[q], vr[q]);
-            if (ownz && e_own[q]) pnew[e_off[q] + sxy * gz] = val;
-          }
-          (&sp[slot][0][0])[e_slot[q]] = val;
-          (&sm[slot][0][0])[(e_slot[q] / FHX) * (FHX + 2) + e_slot[q] % FHX] = vm[q];
-        }
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < FPER; q++) {
-        if (e_slot[q] < FHE) {
-          T val = T(0);
-          if (gz >= 0 && e_off[q] >= 0) {
-            const T z = vr[q] * s_inv[e_cls[q] + wz];
-            val = first ? z : fma(beta, vp[q], z);
-            if (ownz && e_own[q]) pnew[e_off[q] + sxy * gz] = val;
-          }
-          (&sp[slot][0][0])[e_slot[q]] = val;
-          (&sm[slot][0][0])[(e_slot[q] / FHX) * (FHX + 2) + e_slot[q] % FHX] = vm[q];
-        }
-      }
-    }
-  };
-
-  // prologue: planes z0-1 and z0 in the ring, z0+1 in registers
-  issue(z0 - 1);
-  commit(0, z0 - 1);
-  issue(z0);
-  commit(1, z0);
-  issue(z0 + 1);
-
-  const int gx = x0 + tx;
-  const int gy0 = y0 + ty, gy1 = y0 + ty + 8;
-  const bool m0 = gx < nx && gy0 < ny, m1 = gx < nx && gy1 < ny;
-  const int cxy0 = m0 ? wall_count(gx, nx, G.px) + 3 * wall_count(gy0, ny, G.py) : 0;
-  const int cxy1 = m1 ? wall_count(gx, nx, G.px) + 3 * wall_count(gy1, ny, G.py) : 0;
-  typename Acc<T>::type acc = 0;
-
-  for (int z = z0; z < z1; z++) {
-    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
-    commit(st_, z + 1);             // plane z+1 from registers
-    if (z + 2 <= z1) issue(z + 2);  // loads of plane z+2 fly during this plane's work
-    __syncthreads();
-    const int wz = 9 * wall_count(z, nz, G.pz);
-    if (!xy_walls && wz == 0) {
-      // interior plane: diagonal 1, no wall arithmetic
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        if (!(h ? m1 : m0)) continue;
-        const int ly = ty + 1 + 8 * h, lx = tx + 1;
-        const T pc = sp[sc][ly][lx];
-        T a = apply_L<T, ISO>(G, s_dL, 0, pc, sp[sc][ly][lx + 1], sp[sc][ly][lx - 1], sp[sc][ly + 1][lx],
-                              sp[sc][ly - 1][lx], sp[st_][ly][lx], sp[sb][ly][lx]);
-        // a solid cell's row is decoupled; a fluid cell's solid neighbour holds
-        // p = 0, so its coupling vanishes without a select
-        if (MASK && sm[sc][ly][lx]) a = T(0);
-        Ap[gx + (long long)nx * (h ? gy1 : gy0) + sxy * z] = a;
-        acc = fma(pc, a, acc);
-      }
-    } else {
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        if (!(h ? m1 : m0)) continue;
-        const int ly = ty + 1 + 8 * h, lx = tx + 1;
-        const T pc = sp[sc][ly][lx];
-        const int cls = (h ? cxy1 : cxy0) + wz;
-        T a = apply_L<T, ISO>(G, s_dL, cls, pc, sp[sc][ly][lx + 1], sp[sc][ly][lx - 1], sp[sc][ly + 1][lx],
-                              sp[sc][ly - 1][lx], sp[st_][ly][lx], sp[sb][ly][lx]);
-        if (MASK && sm[sc][ly][lx]) a = T(0);
-        Ap[gx + (long long)nx * (h ? gy1 : gy0) + sxy * z] = a;
-        acc = fma(pc, a, acc);
-      }
-    }
-    __syncthreads();
-  }
-  double v[1] = {(double)acc}, tot[1];
-  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
-  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
-    st->pAp = tot[0];
-    st->alpha = st->rz / tot[0];
-    st->first = 0;
-  }
-}
-
 // ------------------------------------------------------------ K1, pairs ---
-// The same search kernel with two x-adjacent cells per thread: a tile is 64 x
-// 16 cells (32 x 8 threads, two rows each).  Halo rows are loaded as aligned
+// K1, the search kernel: p_new = z + beta p_old (z = r on the scaled
+// operator) on the CTA's tile plus a one-cell halo, kept in a 3-plane shared
+// ring while the CTA marches in z; then Ap = L p_new and the (p, Ap) partial.
+// Replaces PP_update_search + exchange + PP_spmv_shared_load + thrust (p,Ap)
+// (src/solver_kernel.cu:528-713,906-927, src/cuda_solver.cu:201-205,256-263).
+// Two x-adjacent cells per thread: a tile is 64 x 16 cells (32 x 8 threads, two rows each).  Halo rows are loaded as aligned
 // pairs into shared rows padded so the pairs stay aligned (index 0 pad, 1 west
 // halo, 2..65 tile, 66 east halo); the two edge columns are scalar loads.
 // Only the thread's own cells need the mask (Ap = 0 in a solid cell), so it
@@ -527,120 +365,6 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
   }
 }
 
-
-// ------------------------------------------------------- K1, cached ---
-// FP32 search kernel without shared-memory staging: each thread forms p_new
-// for its pair of x-adjacent cells and their six neighbours straight from the
-// read-only cache (the FP32 FMAs are cheap, so recomputing a neighbour's p_new
-// costs nothing the memory system notices), then Ap and (p, Ap).  Blocks are
-// 64 x 8 cells of one plane, so y neighbours hit L1 and z neighbours L2; DRAM
-// sees each array about once.  No barriers, no halo bookkeeping.
-template <bool MASK, bool ISO>
-__global__ void __launch_bounds__(FNT) k1_cached(const GeoL G, const float *__restrict__ r,
-                                                 const float *__restrict__ pold, float *__restrict__ pnew,
-                                                 float *__restrict__ Ap, const uint8_t *__restrict__ mask,
-                                                 DevState *st, double *partials) {
-  __shared__ float s_dL[27], s_inv[27];
-  __shared__ double s_red[FNT / 32];
-  if (*(volatile int *)&st->done) return;
-  const bool first = *(volatile int *)&st->first;
-  const float beta = first ? 0.f : (float)(*(volatile double *)&st->beta);
-  load_tabs<float>(G, s_dL, s_inv);
-  __syncthreads();
-  const int nx = G.nx, ny = G.ny, nz = G.nz;
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-  const int gx = blockIdx.x * 64 + 2 * tx, gy = blockIdx.y * 8 + ty, gz = blockIdx.z;
-  float acc = 0.f;
-  if (gx < nx && gy < ny) {
-    const unsigned int plane = (unsigned int)nx * ny;
-    const unsigned int c = plane * gz + (unsigned int)nx * gy + gx;
-    const bool two = gx + 1 < nx;
-    const int wxa = wall_count(gx, nx, G.px), wxb = two ? wall_count(gx + 1, nx, G.px) : 0;
-    const int wyz = 3 * wall_count(gy, ny, G.py) + 9 * wall_count(gz, nz, G.pz);
-    const bool interior = wxa + wxb + wyz == 0;
-    // p_new of a cell from its (r, p_old) and wall class
-    auto pn = [&](unsigned int q, int cls) -> float {
-      float rv = __ldg(r + q);
-      if (cls) rv *= s_inv[cls];
-      return first ? rv : fmaf(beta, __ldg(pold + q), rv);
-    };
-    auto pn2 = [&](unsigned int q, int cla, int clb, float &a, float &b) {
-      if (two && !(q & 1u)) {
-        const float2 rv = __ldg(reinterpret_cast<const float2 *>(r + q));
-        float2 pv = make_float2(0.f, 0.f);
-        if (!first) pv = __ldg(reinterpret_cast<const float2 *>(pold + q));
-        const float ra = cla ? rv.x * s_inv[cla] : rv.x, rb = clb ? rv.y * s_inv[clb] : rv.y;
-        a = fmaf(beta, pv.x, ra);
-        b = fmaf(beta, pv.y, rb);
-      } else {
-        a = pn(q, cla);
-        b = two ? pn(q + 1, clb) : 0.f;
-      }
-    };
-    float c0, c1;
-    pn2(c, wxa + wyz, wxb + wyz, c0, c1);
-    // x neighbours
-    const int xw = halo_index(gx - 1, nx, G.px), xe = halo_index(gx + (two ? 2 : 1), nx, G.px);
-    const unsigned int row = plane * gz + (unsigned int)nx * gy;
-    const float pw = xw >= 0 ? pn(row + xw, wall_count(xw, nx, G.px) + wyz) : 0.f;
-    const float pe = xe >= 0 ? pn(row + xe, wall_count(xe, nx, G.px) + wyz) : 0.f;
-    // y and z neighbours (pairs at the same x)
-    float n0 = 0.f, n1 = 0.f, s0 = 0.f, s1 = 0.f, t0 = 0.f, t1 = 0.f, b0 = 0.f, b1 = 0.f;
-    const int yn = halo_index(gy + 1, ny, G.py), ys = halo_index(gy - 1, ny, G.py);
-    const int zt = halo_index(gz + 1, nz, G.pz), zb = halo_index(gz - 1, nz, G.pz);
-    const int wz = 9 * wall_count(gz, nz, G.pz);
-    if (yn >= 0) {
-      const int cy = 3 * wall_count(yn, ny, G.py) + wz;
-      pn2(plane * gz + (unsigned int)nx * yn + gx, wxa + cy, wxb + cy, n0, n1);
-    }
-    if (ys >= 0) {
-      const int cy = 3 * wall_count(ys, ny, G.py) + wz;
-      pn2(plane * gz + (unsigned int)nx * ys + gx, wxa + cy, wxb + cy, s0, s1);
-    }
-    const int wy = 3 * wall_count(gy, ny, G.py);
-    if (zt >= 0) {
-      const int cz = wy + 9 * wall_count(zt, nz, G.pz);
-      pn2(plane * zt + (unsigned int)nx * gy + gx, wxa + cz, wxb + cz, t0, t1);
-    }
-    if (zb >= 0) {
-      const int cz = wy + 9 * wall_count(zb, nz, G.pz);
-      pn2(plane * zb + (unsigned int)nx * gy + gx, wxa + cz, wxb + cz, b0, b1);
-    }
-    float a0, a1;
-    if (interior) {
-      a0 = apply_L<float, ISO>(G, s_dL, 0, c0, two ? c1 : pe, pw, n0, s0, t0, b0);
-      a1 = apply_L<float, ISO>(G, s_dL, 0, c1, pe, c0, n1, s1, t1, b1);
-    } else {
-      a0 = apply_L<float, ISO>(G, s_dL, wxa + wyz, c0, two ? c1 : pe, pw, n0, s0, t0, b0);
-      a1 = apply_L<float, ISO>(G, s_dL, wxb + wyz, c1, pe, c0, n1, s1, t1, b1);
-    }
-    if (MASK) {
-      if (mask[c]) a0 = 0.f;
-      if (two && mask[c + 1]) a1 = 0.f;
-    }
-    if (two && !(c & 1u)) {
-      *reinterpret_cast<float2 *>(pnew + c) = make_float2(c0, c1);
-      *reinterpret_cast<float2 *>(Ap + c) = make_float2(a0, a1);
-    } else {
-      pnew[c] = c0;
-      Ap[c] = a0;
-      if (two) {
-        pnew[c + 1] = c1;
-        Ap[c + 1] = a1;
-      }
-    }
-    acc = fmaf(c0, a0, acc);
-    if (two) acc = fmaf(c1, a1, acc);
-  }
-  double v[1] = {(double)acc}, tot[1];
-  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
-  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && threadIdx.x == 0) {
-    st->pAp = tot[0];
-    st->alpha = st->rz / tot[0];
-    st->first = 0;
-  }
-}
 
 // ------------------------------------------------------------------ K2 ----
 template <typename T> struct Vec2;

@@ -16,11 +16,12 @@ struct GraphKey {
   int len = 0, replace_every = 0, elem = 0;
   bool rr = false;
   double bscale = 1.0;
+  const void *xhi = nullptr, *rhs64 = nullptr;
   cudaStream_t stream = nullptr;
   bool operator==(const GraphKey &o) const {
     return mask == o.mask && rhs == o.rhs && x == o.x && r == o.r && p0 == o.p0 && p1 == o.p1 && Ap == o.Ap &&
            st == o.st && len == o.len && replace_every == o.replace_every && elem == o.elem && rr == o.rr &&
-           bscale == o.bscale && stream == o.stream;
+           bscale == o.bscale && xhi == o.xhi && rhs64 == o.rhs64 && stream == o.stream;
   }
 };
 
@@ -56,7 +57,6 @@ struct bbpp_ctx {
   int fkz = 1;         // z planes per CTA of the residual kernel
   dim3 fgrid;          // grid of the residual kernel (32x16 tiles)
   int pkz[2] = {1, 1};  // z planes per CTA of the search kernel [FP32, FP64]
-  bool fp32_cached = true;  // FP32 search kernel: cache-fed (true) or z-marching
   dim3 pgrid[2];        // grid of the search kernel (64x16 tiles) [FP32, FP64]
   int egrid = 1;       // elementwise grid (1-D)
   size_t nparts = 0;   // capacity of partials (per sum)
@@ -105,6 +105,7 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
                   bbpp_report *rep);
 void bbpp_ir_free(bbpp_ctx *ctx);
 
+void bbpp_set_reliable(double *xhi, const double *rhs);
 int bbpp_residual_async(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x, double *r);
 
 // learned initial guess (bbpp_net.cu)

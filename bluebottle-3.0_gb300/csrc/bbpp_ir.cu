@@ -1,6 +1,8 @@
-// bbpp_ir.cu -- FP32-inner / FP64 iterative-refinement PCG.
+// bbpp_ir.cu -- FP32-inner / FP64 iterative-refinement PCG, in two forms:
+// reliable updates (default, below) and restarted refinement.
 //
-// Outer loop (FP64): r = rhs - (-A)x, stop when ||r|| <= tol ||rhs||.
+// Restarted refinement: outer loop (FP64): r = rhs - (-A)x, stop when
+// ||r|| <= tol ||rhs||.
 // Inner sweep (FP32 vectors, FP64 dot accumulators across threads and CTAs):
 // Jacobi PCG on (-A)d = r from d = 0 until ||r_d|| <= inner_tol ||r||, then
 // x += d in FP64.  The inner sweeps reuse the FP64 method's kernels
@@ -49,8 +51,78 @@ __global__ void k_add_correction(const Geo G, double *__restrict__ x, const floa
     x[c] += (double)d[c];
 }
 
+static int ensure_ir(bbpp_ctx *ctx);
+
+// Reliable-update form: one FP32 PCG on L d = S rhs - L x; every residual
+// replacement (and the confirmation of a recursive convergence) adds d into x
+// in FP64, zeroes d and recomputes the residual from x in FP64.  The search
+// direction is kept, so nothing of the Krylov space is lost to restarts.
+static int solve_reliable(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o,
+                          bool zero_x, bbpp_report *rep) {
+  const size_t n = (size_t)ctx->G.n;
+  int rc = ensure_ir(ctx);
+  if (rc) return rc;
+  IrBuffers *b = ctx->ir;
+  DevState *st = ctx->st, *hst = ctx->hst;
+  const double S = ctx->GL.S;
+  if (zero_x) CK(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+  memset(hst, 0, sizeof(DevState));
+  hst->tol2bb = o->tol * o->tol * (o->stop == 0 ? S : S * S);
+  hst->tiny = 1e-16;
+  hst->max_iter = o->max_iter;
+  hst->stop = o->stop;
+  hst->first = 1;
+  CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(b->d, 0, sizeof(float) * n, ctx->stream));
+  bbpp_launch_resid_s<double, float>(ctx, mask, x, rhs, b->rd, st, RES_INIT, S);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  bbpp_set_reliable(x, rhs);
+  float *const p[2] = {b->p[0], b->p[1]};
+  int it = 0;
+  rc = bbpp_pcg_loop<float>(ctx, mask, b->r, b->d, b->rd, p, b->Ap, st, hst, o->replace_every,
+                            o->stop == BBPP_STOP_TRUE_REL, true, &it);
+  bbpp_set_reliable(nullptr, nullptr);
+  if (rc) return rc;
+  k_add_correction<<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, b->d);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  rep->iters = it;
+  rep->outer = hst->replacements;
+  rep->replacements = hst->replacements;
+  rep->bb = hst->bb;
+  rep->rz = hst->rz_last / S;
+  rep->rel_resid = hst->bb > 0 ? std::sqrt(std::max(0.0, hst->rr) / hst->bb) / S : 0.0;
+  switch (hst->done) {
+    case DONE_CONVERGED: rep->status = BBPP_CONVERGED; break;
+    case DONE_TINY: rep->status = BBPP_TINY_RHS; break;
+    case DONE_NAN: rep->status = BBPP_NAN; break;
+    default: rep->status = BBPP_MAX_ITER;
+  }
+  // bytes: 41 B/cell per FP32 iteration; each reliable update folds (12) and
+  // forms the FP64 residual (21); the initial residual and final fold likewise
+  rep->bytes = (double)n * (41.0 * it + 33.0 * (hst->replacements + 1));
+  return 0;
+}
+
+static int ensure_ir(bbpp_ctx *ctx) {
+  const size_t n = (size_t)ctx->G.n;
+  if (!ctx->ir) {
+    IrBuffers *b = new IrBuffers();
+    ctx->ir = b;
+    CK(cudaMalloc(&b->r, sizeof(float) * n));
+    CK(cudaMalloc(&b->d, sizeof(float) * n));
+    CK(cudaMalloc(&b->rd, sizeof(float) * n));
+    CK(cudaMalloc(&b->p[0], sizeof(float) * n));
+    CK(cudaMalloc(&b->p[1], sizeof(float) * n));
+    CK(cudaMalloc(&b->Ap, sizeof(float) * n));
+  }
+  return 0;
+}
+
 int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double *x, const bbpp_opts *o, bool zero_x,
                   bbpp_report *rep) {
+  if (o->ir_mode == BBPP_IR_RELIABLE) return solve_reliable(ctx, mask, rhs, x, o, zero_x, rep);
   const size_t n = (size_t)ctx->G.n;
   if (!ctx->ir) {
     IrBuffers *b = new IrBuffers();

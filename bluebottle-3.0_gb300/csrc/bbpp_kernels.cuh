@@ -1,16 +1,8 @@
-// bbpp_kernels.cuh -- the PCG kernels, templated on the vector type T
-// (double for the FP64 method, float for the inner sweeps of FP32_IR).
+// bbpp_kernels.cuh -- general-form kernels on the unscaled operator (-A),
+// templated on the vector type.  The PCG iteration itself runs on the scaled
+// operator in bbpp_fast.cuh; these serve the kernel-level entry points
+// (SpMV, residual, the context-free residual) and the checks.
 //
-//  k_search_spmv  (K1): p_new = invM r + beta p_old on the CTA's tile plus a
-//                 one-cell halo, stored to a 3-plane shared ring while the CTA
-//                 marches in z; then Ap = (-A) p_new and the (p, Ap) partial.
-//                 Replaces PP_update_search + exchange + PP_spmv_shared_load +
-//                 thrust (p,Ap) (src/solver_kernel.cu:528-713,906-927,
-//                 src/cuda_solver.cu:201-205,256-263).
-//  k_update       (K2): x += alpha p, r -= alpha Ap, z = invM r on the fly,
-//                 (r,z) and (r,r) partials.  Replaces PP_update_soln_resid +
-//                 thrust (r,z) (src/solver_kernel.cu:838-862,
-//                 src/cuda_solver.cu:226-232).
 //  k_axpy_x       x += alpha p (PP_update_solution, src/solver_kernel.cu:864-881).
 //  k_resid        r = rhs - (-A) x with (r,z), (r,r), (rhs,rhs) partials
 //                 (PP_update_residual after an SpMV of phi,
@@ -36,130 +28,6 @@ enum ResidMode : int { RES_INIT = 0, RES_ITER = 1, RES_CONFIRM = 2, RES_PLAIN = 
 
 __device__ __forceinline__ void load_tab(const Geo &G, double *s_tab) {
   for (int e = threadIdx.x; e < 81; e += blockDim.x) s_tab[e] = G.tab[e];
-}
-
-// ----------------------------------------------------------------- K1 -----
-template <typename T, bool MASK>
-__global__ void __launch_bounds__(NT) k_search_spmv(const Geo G, const T *__restrict__ r,
-                                                    const T *__restrict__ pold, T *__restrict__ pnew,
-                                                    T *__restrict__ Ap, const uint8_t *__restrict__ mask,
-                                                    DevState *st, double *partials, int kz) {
-  __shared__ double s_tab[81];
-  __shared__ T sp[3][HY][HX];
-  __shared__ uint8_t sm[3][HY][HX + 2];
-  __shared__ double s_red[NT / 32];
-  if (*(volatile int *)&st->done) return;
-  const bool first = *(volatile int *)&st->first;
-  const T beta = first ? T(0) : (T)(*(volatile double *)&st->beta);
-  load_tab(G, s_tab);
-
-  const int tid = threadIdx.x;
-  const int tx = tid & (TX - 1), ty = tid / TX;
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-  const int z0 = blockIdx.z * kz;
-  const int z1 = min(z0 + kz, G.nz);
-  const int nx = G.nx, ny = G.ny, nz = G.nz;
-  __syncthreads();
-
-  auto load_plane = [&](int slot, int zr, bool own) {
-    const int gz = halo_index(zr, nz, G.pz);
-    for (int e = tid; e < HX * HY; e += NT) {
-      const int ly = e / HX, lx = e - ly * HX;
-      const int rx = x0 + lx - 1, ry = y0 + ly - 1;
-      const int gx = halo_index(rx, nx, G.px), gy = halo_index(ry, ny, G.py);
-      T val = T(0);
-      uint8_t m = 0;
-      if (gz >= 0 && gx >= 0 && gy >= 0) {
-        const long long c = gx + (long long)nx * (gy + (long long)ny * gz);
-        const int cls = wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py) + 9 * wall_count(gz, nz, G.pz);
-        const T z = (T)s_tab[27 + cls] * r[c];
-        val = first ? z : fma(beta, pold[c], z);
-        if (MASK) m = mask[c];
-        if (own && rx == gx && ry == gy && lx >= 1 && lx <= TX && ly >= 1 && ly <= TY) pnew[c] = val;
-      }
-      sp[slot][ly][lx] = val;
-      sm[slot][ly][lx] = m;
-    }
-  };
-
-  typename Acc<T>::type acc = 0;
-  load_plane(0, z0 - 1, false);
-  load_plane(1, z0, true);
-  const T cx = (T)G.cx, cy = (T)G.cy, cz = (T)G.cz;
-  const int gx = x0 + tx, gy = y0 + ty;
-  const bool mine = gx < nx && gy < ny;
-  const int cls_xy = mine ? (wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py)) : 0;
-  for (int z = z0; z < z1; z++) {
-    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
-    load_plane(st_, z + 1, z + 1 < z1);
-    __syncthreads();
-    if (mine) {
-      T pc = sp[sc][ty + 1][tx + 1];
-      T pe = sp[sc][ty + 1][tx + 2], pw = sp[sc][ty + 1][tx];
-      T pn = sp[sc][ty + 2][tx + 1], ps = sp[sc][ty][tx + 1];
-      T pt = sp[st_][ty + 1][tx + 1], pb = sp[sb][ty + 1][tx + 1];
-      const int cls = cls_xy + 9 * wall_count(z, nz, G.pz);
-      T d = (T)s_tab[cls];
-      if (MASK) {
-        const bool mc = sm[sc][ty + 1][tx + 1] != 0;
-        pe = (mc || sm[sc][ty + 1][tx + 2]) ? T(0) : pe;
-        pw = (mc || sm[sc][ty + 1][tx]) ? T(0) : pw;
-        pn = (mc || sm[sc][ty + 2][tx + 1]) ? T(0) : pn;
-        ps = (mc || sm[sc][ty][tx + 1]) ? T(0) : ps;
-        pt = (mc || sm[st_][ty + 1][tx + 1]) ? T(0) : pt;
-        pb = (mc || sm[sb][ty + 1][tx + 1]) ? T(0) : pb;
-        d = mc ? (T)s_tab[54 + cls] : d;
-      }
-      T s = cx * (pe + pw);
-      s = fma(cy, pn + ps, s);
-      s = fma(cz, pt + pb, s);
-      const T a = fma(d, pc, -s);
-      const long long c = gx + (long long)nx * (gy + (long long)ny * z);
-      Ap[c] = a;
-      acc = fma(pc, a, acc);
-    }
-    __syncthreads();
-  }
-  double v[1] = {(double)acc}, tot[1];
-  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
-  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
-    st->pAp = tot[0];
-    st->alpha = st->rz / tot[0];
-    st->first = 0;
-  }
-}
-
-// ----------------------------------------------------------------- K2 -----
-template <typename T, bool RR>
-__global__ void __launch_bounds__(NT) k_update(const Geo G, T *__restrict__ x, T *__restrict__ r,
-                                               const T *__restrict__ p, const T *__restrict__ Ap,
-                                               DevState *st, double *partials) {
-  __shared__ double s_tab[81];
-  __shared__ double s_red[2 * NT / 32];
-  if (*(volatile int *)&st->done) return;
-  const T alpha = (T)(*(volatile double *)&st->alpha);
-  load_tab(G, s_tab);
-  __syncthreads();
-  typename Acc<T>::type rz = 0, rr = 0;
-  const unsigned int n = (unsigned int)G.n;
-  for (unsigned int c = blockIdx.x * NT + threadIdx.x; c < n; c += gridDim.x * NT) {
-    const unsigned int row = fdiv(c, G.mx);
-    const unsigned int k = fdiv(c, G.mxy);
-    const int i = (int)(c - row * (unsigned)G.nx);
-    const int j = (int)(row - k * (unsigned)G.ny);
-    const int cls = wall_count(i, G.nx, G.px) + 3 * wall_count(j, G.ny, G.py) + 9 * wall_count((int)k, G.nz, G.pz);
-    const T pv = p[c], av = Ap[c];
-    x[c] = fma(alpha, pv, x[c]);
-    const T rn = fma(-alpha, av, r[c]);
-    r[c] = rn;
-    const T zv = (T)s_tab[27 + cls] * rn;
-    rz = fma(rn, zv, rz);
-    if (RR) rr = fma(rn, rn, rr);
-  }
-  double v[2] = {(double)rz, (double)rr}, tot[2];
-  if (last_cta_reduce<2>(v, partials, st, gridDim.x, blockIdx.x, s_red, tot) && threadIdx.x == 0)
-    finish_iteration(st, tot[0], RR ? tot[1] : 0.0, true);
 }
 
 template <typename T>

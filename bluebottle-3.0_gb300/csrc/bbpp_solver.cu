@@ -193,7 +193,7 @@ static void stencil_shape(bbpp_ctx *ctx) {
   const int gx = (G.nx + TX - 1) / TX, gy = (G.ny + TY - 1) / TY;
   // enough CTAs for one full wave of resident CTAs, each marching kz planes
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_search_spmv<double, true>, NT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resid<double, double, true>, NT, 0);
   if (per_sm < 1) per_sm = 1;
   const long long target = (long long)ctx->sms * per_sm;
   int nzc = (int)std::max<long long>(1, target / std::max(1, gx * gy));
@@ -206,7 +206,7 @@ static void stencil_shape(bbpp_ctx *ctx) {
   {
     const int fx = (G.nx + FX - 1) / FX, fy = (G.ny + FY - 1) / FY;
     int pf = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k1_search<double, true, true>, FNT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k_resid_s<double, double, true, true>, FNT, 0);
     if (pf < 1) pf = 1;
     const long long tgt = (long long)ctx->sms * pf;
     int nzf = (int)std::max<long long>(1, tgt / std::max(1, fx * fy));
@@ -236,7 +236,7 @@ static void stencil_shape(bbpp_ctx *ctx) {
     ctx->pgrid[prec] = dim3(fx, fy, nzf);
   }
   int per_sm2 = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_update<double, true>, NT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k2_update<double>, FNT, 0);
   if (per_sm2 < 1) per_sm2 = 1;
   long long eb = std::min<long long>((G.n + NT - 1) / NT, (long long)ctx->sms * per_sm2);
   ctx->egrid = (int)std::max<long long>(1, eb);
@@ -259,10 +259,6 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
   ctx->grid = *g;
   geol_init(ctx->G, &ctx->GL);
   ctx->sms = dev_sms();
-  {
-    const char *e = getenv("BBPP_FP32_SEARCH");  // "marched" selects the z-marching FP32 kernel
-    ctx->fp32_cached = !(e && strcmp(e, "marched") == 0);
-  }
   stencil_shape(ctx);
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
@@ -349,6 +345,7 @@ extern "C" void bbpp_default_opts(bbpp_opts *o) {
   o->replace_every = 50;
   o->inner_tol = 1e-4;
   o->max_outer = 30;
+  o->ir_mode = BBPP_IR_RELIABLE;
   o->net = nullptr;
   o->prev = nullptr;
 }
@@ -376,19 +373,6 @@ extern "C" const char *bbpp_version(void) { return "bbpp 0.1 (sm_103a)"; }
 
 // ---------------------------------------------------------------- launches --
 // All launches go to ctx->stream.  Typed on the vector element.
-static void launch_search_cached(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const float *pold,
-                                 float *pnew, float *Ap, DevState *st) {
-  const dim3 g((ctx->G.nx + 63) / 64, (ctx->G.ny + 7) / 8, ctx->G.nz);
-  cudaStream_t s = ctx->stream;
-  if (mask) {
-    if (ctx->GL.iso) k1_cached<true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
-    else k1_cached<true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
-  } else {
-    if (ctx->GL.iso) k1_cached<false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
-    else k1_cached<false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials);
-  }
-}
-
 template <typename T>
 static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap,
                                DevState *st) {
@@ -396,9 +380,7 @@ static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, c
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_SEARCH_SPMV : KK_SEARCH_SPMV_F32, 4.0 * sizeof(T) + (mask ? 1 : 0));
   const int prec = sizeof(T) == 8 ? 1 : 0;
   cudaStream_t s = ctx->stream;
-  if (prec == 0 && ctx->fp32_cached) {
-    launch_search_cached(ctx, mask, (const float *)r, (const float *)pold, (float *)pnew, (float *)Ap, st);
-  } else {
+  {
     const dim3 g = ctx->pgrid[prec];
     const int kz = ctx->pkz[prec];
     if (mask) {
@@ -473,6 +455,42 @@ template void bbpp_launch_resid_s<float, float>(bbpp_ctx *, const uint8_t *, flo
 // rhs, 1 for an already scaled one)
 static thread_local double t_bscale = 1.0;
 
+// Reliable updates of the mixed-precision solve: when set, the FP32 loop's
+// residual replacements and confirmations fold the FP32 correction into the
+// FP64 solution and recompute the residual from it in FP64.
+struct Reliable {
+  double *xhi = nullptr;
+  const double *rhs = nullptr;
+};
+static thread_local Reliable t_rel;
+
+void bbpp_set_reliable(double *xhi, const double *rhs) {
+  t_rel.xhi = xhi;
+  t_rel.rhs = rhs;
+}
+
+// x_hi += d; d = 0 (kernels of a finished solve return at once when check)
+__global__ void k_fold(const GeoL G, double *__restrict__ xhi, float *__restrict__ d, const DevState *st,
+                       int check) {
+  if (check && *(volatile const int *)&st->done) return;
+  const unsigned int n = (unsigned int)G.n;
+  for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    xhi[c] += (double)d[c];
+    d[c] = 0.f;
+  }
+}
+
+// the residual step of an iteration or a confirmation, for vectors of type T
+template <typename T>
+static void launch_replace(bbpp_ctx *ctx, const uint8_t *mask, T *x, const T *rhs, T *r, DevState *st, int mode) {
+  if (sizeof(T) == 4 && t_rel.xhi) {
+    k_fold<<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, t_rel.xhi, (float *)x, st, mode == RES_ITER);
+    bbpp_launch_resid_s<double, float>(ctx, mask, t_rel.xhi, t_rel.rhs, (float *)r, st, mode, ctx->GL.S);
+  } else {
+    bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, mode, t_bscale);
+  }
+}
+
 template <typename T>
 static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
                              DevState *st, int q, int replace_every, bool rr) {
@@ -483,7 +501,7 @@ static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T
     bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_AXPY : KK_AXPY_F32, 3.0 * sizeof(T));
     k_axpy2<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, pnew, st);
     bbpp_rec_end(ctx);
-    bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, RES_ITER, t_bscale);
+    launch_replace<T>(ctx, mask, x, rhs, r, st, RES_ITER);
   } else {
     launch_update<T>(ctx, x, r, pnew, Ap, st, rr);
   }
@@ -508,6 +526,8 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   key.elem = (int)sizeof(T);
   key.stream = ctx->stream;
   key.bscale = t_bscale;
+  key.xhi = t_rel.xhi;
+  key.rhs64 = t_rel.rhs;
   for (auto &gc : ctx->graphs)
     if (gc.key == key) {
       *out = gc.exec;
@@ -600,7 +620,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
       for (int i = 1; i <= chunk; i++) {
         ctx->rec_iter = i;
         launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, q + i, replace_every, rr);
-        ctx->launches += ((q + i) % replace_every == 0) ? 3 : 2;
+        ctx->launches += ((q + i) % replace_every == 0) ? (t_rel.xhi ? 4 : 3) : 2;
       }
       ctx->rec = nullptr;
       CK(cudaGetLastError());
@@ -609,7 +629,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
       ctx->rec_iter = 1;
       launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, q + 1, replace_every, rr);
       ctx->rec = nullptr;
-      ctx->launches += ((q + 1) % replace_every == 0) ? 3 : 2;
+      ctx->launches += ((q + 1) % replace_every == 0) ? (t_rel.xhi ? 4 : 3) : 2;
       CK(cudaGetLastError());
     }
     CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
@@ -625,8 +645,8 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
         CK(cudaMemcpyAsync(&st->done, &hst->done, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
         break;
       }
-      bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, RES_CONFIRM, t_bscale);
-      ctx->launches += 1;
+      launch_replace<T>(ctx, mask, x, rhs, r, st, RES_CONFIRM);
+      ctx->launches += (sizeof(T) == 4 && t_rel.xhi) ? 2 : 1;
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
@@ -675,6 +695,7 @@ static int check_opts(const bbpp_opts *o) {
   if (o->precision != BBPP_FP64 && o->precision != BBPP_FP32_IR) return BBPP_BAD_ARG;
   if (o->guess < BBPP_GUESS_ZERO || o->guess > BBPP_GUESS_LEARNED) return BBPP_BAD_ARG;
   if (o->stop != BBPP_STOP_REF_RZ && o->stop != BBPP_STOP_TRUE_REL) return BBPP_BAD_ARG;
+  if (o->ir_mode != BBPP_IR_RELIABLE && o->ir_mode != BBPP_IR_RESTART) return BBPP_BAD_ARG;
   if (!(o->tol >= 0) || o->max_iter < 0 || o->replace_every < 1) return BBPP_BAD_ARG;
   if (o->guess == BBPP_GUESS_LEARNED && !o->net) return BBPP_BAD_ARG;
   return 0;

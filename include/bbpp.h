@@ -67,6 +67,12 @@ typedef enum bbpp_guess {
   BBPP_GUESS_LEARNED = 2  /* x0 from the learned network (bbpp_net_*) */
 } bbpp_guess;
 
+typedef enum bbpp_ir_mode {
+  BBPP_IR_RELIABLE = 0,  /* one FP32 PCG run; its residual replacements fold the FP32 correction into the
+                            FP64 solution and recompute the residual in FP64 (no Krylov restart) */
+  BBPP_IR_RESTART = 1    /* classic refinement: an FP32 PCG per outer FP64 residual, restarted each sweep */
+} bbpp_ir_mode;
+
 typedef enum bbpp_stop {
   BBPP_STOP_REF_RZ = 0,   /* (r,z) <= tol^2 (rhs,rhs): the reference rule (src/cuda_solver.cu:235) */
   BBPP_STOP_TRUE_REL = 1  /* ||rhs-(-A)x|| / ||rhs|| <= tol, confirmed with an explicit residual */
@@ -79,10 +85,11 @@ typedef struct bbpp_opts {
   double tol;         /* pp_residual (REF_RZ) or relative residual (TRUE_REL) */
   int max_iter;       /* pp_max_iter; at most max_iter+1 iterations, as the reference */
   int replace_every;  /* explicit residual every n iterations (50 in the reference) */
-  double inner_tol;   /* FP32_IR: relative residual reduction per refinement sweep */
-  int max_outer;      /* FP32_IR: refinement sweeps */
+  double inner_tol;   /* FP32_IR restart mode: relative residual reduction per sweep */
+  int max_outer;      /* FP32_IR restart mode: refinement sweeps */
   void *net;          /* GUESS_LEARNED: a bbpp_net handle */
   const double *prev; /* GUESS_LEARNED: previous pressure (device), may be NULL */
+  int ir_mode;        /* FP32_IR: bbpp_ir_mode */
 } bbpp_opts;
 
 typedef struct bbpp_report {

@@ -159,13 +159,14 @@ def test_warm_start_and_repeat(lib, orc):
     assert r3.status == bbpp.CONVERGED and r3.iters <= 1
 
 
+@pytest.mark.parametrize("ir_mode", [bbpp.IR_RELIABLE, bbpp.IR_RESTART])
 @pytest.mark.parametrize("name,n,tol", [("C2", 64, 1e-8), ("C3", 96, 1e-8), ("C1", 32, 1e-10)])
-def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol):
+def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol, ir_mode):
     g, mask, rhs, _ = problems.make_problem(name, n=n)
     s = bbpp.Solver(g)
-    x, rep = s.solve_host(rhs, mask, tol=tol, precision=bbpp.FP32_IR)
+    x, rep = s.solve_host(rhs, mask, tol=tol, precision=bbpp.FP32_IR, ir_mode=ir_mode)
     assert rep.status == bbpp.CONVERGED and rep.true_rel <= tol * 1.01
-    assert rep.outer >= 1
+    assert rep.outer >= 1  # refinement sweeps, or reliable updates (the confirmation is one)
     xo, res = orc.pcg(to_orc(orc, g), rhs, mask, tol=1e-13)
     if mask is None:
         x, xo = x - x.mean(), xo - xo.mean()
@@ -175,10 +176,12 @@ def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol):
 
 
 @pytest.mark.parametrize("dims,bc", SHAPES)
-@pytest.mark.parametrize("precision", [bbpp.FP64, bbpp.FP32_IR])
-def test_solve_odd_shapes(lib, orc, dims, bc, precision):
+@pytest.mark.parametrize("precision,ir_mode", [(bbpp.FP64, 0), (bbpp.FP32_IR, bbpp.IR_RELIABLE),
+                                               (bbpp.FP32_IR, bbpp.IR_RESTART)])
+def test_solve_odd_shapes(lib, orc, dims, bc, precision, ir_mode):
     """Whole solves on odd, tile-edge and tiny grids with every boundary mix,
-    masked, through both search kernels (FP64 z-marching, FP32 cache-fed)."""
+    masked, in FP64 and in both mixed-precision forms (the search kernel's
+    pair and scalar paths, partial tiles, wall classes)."""
     nx, ny, nz = dims
     g = bbpp.Grid.make(nx, ny, nz, 1.0 / nx, 1.0 / ny, 1.0 / nz, bc)
     mask = rand_mask(g.shape, nx + ny, 0.1)
@@ -188,7 +191,7 @@ def test_solve_odd_shapes(lib, orc, dims, bc, precision):
     b[mask == 0] -= b[mask == 0].mean()
     s = bbpp.Solver(g)
     tol = 1e-10 if precision == bbpp.FP64 else 1e-8
-    x, rep = s.solve_host(b, mask, tol=tol, precision=precision)
+    x, rep = s.solve_host(b, mask, tol=tol, precision=precision, ir_mode=ir_mode)
     assert rep.status == bbpp.CONVERGED and rep.true_rel <= tol * 1.01
     xo, res = orc.pcg(to_orc(orc, g), b, mask, tol=1e-13)
     assert np.all(x[mask == 1] == 0)
