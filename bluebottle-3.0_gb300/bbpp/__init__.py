@@ -111,6 +111,7 @@ def lib():
         "bbpp_solve_host": (I, [P, P, P, P, ctypes.POINTER(Opts), ctypes.POINTER(Report)]),
         "bbpp_spmv": (I, [P, P, P, P]),
         "bbpp_invm": (I, [P, P]),
+        "bbpp_search_step": (I, [P, I, I, P, P, P, P, P, P, D, D, I, I, ctypes.POINTER(D)]),
         "bbpp_residual": (I, [P, P, P, P, P, ctypes.POINTER(D), ctypes.POINTER(D)]),
         "bbpp_sphere_mask": (I, [P, D, D, D, I, P, P, P, P, P]),
         "bbpp_dev_alloc": (I, [S, ctypes.POINTER(P)]),
@@ -252,6 +253,16 @@ class Solver:
 
     def spmv(self, p, Ap, mask=None):
         _check(lib().bbpp_spmv(self.handle, _ptr(mask), _ptr(p), _ptr(Ap)), self.handle)
+
+    def search_step(self, r, pold, pnew, Ap, x, mask=None, beta=0.0, alpha=0.0, first=False, lag=False,
+                    precision=FP64, kernel=0):
+        """One search-kernel launch (kernel 0 = the solver's choice, 1 = z-marching tiles,
+        2 = TMA-staged, FP32 only); returns (p_new, Ap)."""
+        pAp = ctypes.c_double()
+        _check(lib().bbpp_search_step(self.handle, precision, kernel, _ptr(mask), _ptr(r), _ptr(pold), _ptr(pnew),
+                                      _ptr(Ap), _ptr(x), beta, alpha, int(first), int(lag), ctypes.byref(pAp)),
+               self.handle)
+        return pAp.value
 
     def invm(self, out):
         _check(lib().bbpp_invm(self.handle, _ptr(out)), self.handle)

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", INC, "-I", CSRC]
 
-CORE = ["bbpp_solver.cu", "bbpp_ir.cu", "bbpp_net.cu", "bbpp_noalloc.cu"]
+CORE = ["bbpp_solver.cu", "bbpp_ir.cu", "bbpp_net.cu", "bbpp_noalloc.cu", "bbpp_tma.cu"]
 DROPIN = ["bbpp_bluebottle.cu"]
 
 

@@ -19,7 +19,8 @@ enum DoneCode : int {
   DONE_MAX_ITER = 2,
   DONE_NAN = 3,
   DONE_PENDING = 4,  // recursive residual met TRUE_REL; explicit check pending
-  DONE_TINY = 5
+  DONE_TINY = 5,
+  DONE_TIMEOUT = 6   // a bounded wait inside a kernel ran out
 };
 
 // Device-resident scalar state of one PCG solve.
@@ -39,7 +40,7 @@ struct DevState {
   int stop;        // 0 = (r,z) rule, 1 = recursive ||r|| rule + explicit confirm
   int replacements;
   unsigned int ticket;  // arrival counter of the last-CTA reductions
-  int pad;
+  int dlag;        // x lacks alpha * p of the last search direction (added by the next search kernel)
   double tiny;     // (rhs,rhs) below this ends the solve at once (DONE_TINY)
 };
 

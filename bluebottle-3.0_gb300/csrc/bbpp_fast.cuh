@@ -114,9 +114,32 @@ template <typename T> struct V2of;
 template <> struct V2of<double> { typedef double2 type; };
 template <> struct V2of<float> { typedef float2 type; };
 
+// Own cells of a committed plane: store p_new, and add the previous
+// iteration's alpha p_old into x while p_old is at hand (x lags one step).
+template <typename T, typename V2>
+__device__ __forceinline__ void store_own(T *__restrict__ pnew, T *__restrict__ x, unsigned int c, const V2 v,
+                                          const T (&po)[2], T alpha, bool lag, bool pair_full, int npair) {
+  if (pair_full) {
+    *reinterpret_cast<V2 *>(pnew + c) = v;
+    if (lag) {
+      V2 xv = *reinterpret_cast<const V2 *>(x + c);
+      xv.x = fma(alpha, po[0], xv.x);
+      xv.y = fma(alpha, po[1], xv.y);
+      *reinterpret_cast<V2 *>(x + c) = xv;
+    }
+  } else {
+    pnew[c] = v.x;
+    if (lag) x[c] = fma(alpha, po[0], x[c]);
+    if (npair == 2) {
+      pnew[c + 1] = v.y;
+      if (lag) x[c + 1] = fma(alpha, po[1], x[c + 1]);
+    }
+  }
+}
+
 template <typename T, bool MASK, bool ISO>
 __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const GeoL G, const T *__restrict__ r, const T *__restrict__ pold,
-                                                  T *__restrict__ pnew, T *__restrict__ Ap,
+                                                  T *__restrict__ pnew, T *__restrict__ Ap, T *__restrict__ x,
                                                   const uint8_t *__restrict__ mask, DevState *st, double *partials,
                                                   int kz) {
   typedef typename V2of<T>::type V2;
@@ -126,6 +149,9 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
   if (*(volatile int *)&st->done) return;
   const bool first = *(volatile int *)&st->first;
   const T beta = first ? T(0) : (T)(*(volatile double *)&st->beta);
+  // x += alpha p_old of the previous iteration, on the own cells as p_old passes
+  const bool lag = !first && *(volatile int *)&st->dlag;
+  const T alpha = lag ? (T)(*(volatile double *)&st->alpha) : T(0);
   load_tabs<T>(G, s_dL, s_inv);
 
   const int tid = threadIdx.x;
@@ -232,12 +258,7 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
         *reinterpret_cast<V2 *>(&sp[slot][ly][2 + 2 * tx]) = v;
         if (ownz && ly >= 1 && ly <= PY && row_off[k] >= 0 && y0 + ly - 1 < ny && npair > 0) {
           const unsigned int c = zoff + (unsigned int)row_off[k] + (unsigned int)gxp;
-          if (pair_full) {
-            *reinterpret_cast<V2 *>(pnew + c) = v;
-          } else {
-            pnew[c] = v.x;
-            if (npair == 2) pnew[c + 1] = v.y;
-          }
+          store_own<T, V2>(pnew, x, c, v, vp[k], alpha, lag, pair_full, npair);
         }
       }
     } else {
@@ -256,12 +277,7 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
         *reinterpret_cast<V2 *>(&sp[slot][ly][2 + 2 * tx]) = v;
         if (ownz && ly >= 1 && ly <= PY && row_off[k] >= 0 && y0 + ly - 1 < ny && npair > 0) {
           const unsigned int c = zoff + (unsigned int)row_off[k] + (unsigned int)gxp;
-          if (pair_full) {
-            *reinterpret_cast<V2 *>(pnew + c) = v;
-          } else {
-            pnew[c] = v.x;
-            if (npair == 2) pnew[c + 1] = v.y;
-          }
+          store_own<T, V2>(pnew, x, c, v, vp[k], alpha, lag, pair_full, npair);
         }
       }
     }
@@ -362,6 +378,7 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
     st->pAp = tot[0];
     st->alpha = st->rz / tot[0];
     st->first = 0;
+    st->dlag = 1;
   }
 }
 
@@ -380,30 +397,25 @@ __device__ __forceinline__ int cell_class(const GeoL &G, unsigned int c) {
   return wall_count(i, G.nx, G.px) + 3 * wall_count(j, G.ny, G.py) + 9 * wall_count((int)k, G.nz, G.pz);
 }
 
-// One pair of cells: x += alpha p, r -= alpha Ap; returns the new r.
+// One pair of cells: r -= alpha Ap; returns the new r.
 template <typename T, typename V2>
-__device__ __forceinline__ V2 update_pair(unsigned int q, T alpha, T *__restrict__ x, T *__restrict__ r,
-                                          const T *__restrict__ p, const T *__restrict__ Ap) {
-  const V2 pv = reinterpret_cast<const V2 *>(p)[q];
+__device__ __forceinline__ V2 update_pair(unsigned int q, T alpha, T *__restrict__ r, const T *__restrict__ Ap) {
   const V2 av = reinterpret_cast<const V2 *>(Ap)[q];
-  V2 xv = reinterpret_cast<V2 *>(x)[q];
   V2 rv = reinterpret_cast<V2 *>(r)[q];
-  xv.x = fma(alpha, pv.x, xv.x);
-  xv.y = fma(alpha, pv.y, xv.y);
   rv.x = fma(-alpha, av.x, rv.x);
   rv.y = fma(-alpha, av.y, rv.y);
-  reinterpret_cast<V2 *>(x)[q] = xv;
   reinterpret_cast<V2 *>(r)[q] = rv;
   return rv;
 }
 
+// K2: r -= alpha Ap with (r,z) and (r,r); x += alpha p is left to the next
+// search kernel (or the settle / fold kernels), which reads p anyway.
 // (r,z) = (r,r) + sum over wall cells of (invL - 1) r^2.  Cells of interior
 // planes carry no class arithmetic: with periodic x and y the pairs of the two
 // z-wall planes run in loops of their own with one weight each.
 template <typename T>
-__global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x, T *__restrict__ r,
-                                                 const T *__restrict__ p, const T *__restrict__ Ap, DevState *st,
-                                                 double *partials) {
+__global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r, const T *__restrict__ Ap,
+                                                 DevState *st, double *partials) {
   __shared__ T s_dL[27], s_inv[27];
   __shared__ double s_red[2 * FNT / 32];
   if (*(volatile int *)&st->done) return;
@@ -421,7 +433,7 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x
     const unsigned int wall_lo = G.pz ? 0u : plane / 2;                  // pairs in plane 0
     const unsigned int wall_hi = G.pz ? n / 2 : (n - plane) / 2;         // first pair of plane nz-1
     for (unsigned int q = wall_lo + t0; q < wall_hi; q += stride) {
-      const V2 rv = update_pair<T, V2>(q, alpha, x, r, p, Ap);
+      const V2 rv = update_pair<T, V2>(q, alpha, r, Ap);
       rr = fma(rv.x, rv.x, rr);
       rr = fma(rv.y, rv.y, rr);
     }
@@ -429,14 +441,14 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x
       const int wc = 9 * (G.nz == 1 ? 2 : 1);
       const T w = s_inv[wc] - T(1);
       for (unsigned int q = t0; q < wall_lo; q += stride) {
-        const V2 rv = update_pair<T, V2>(q, alpha, x, r, p, Ap);
+        const V2 rv = update_pair<T, V2>(q, alpha, r, Ap);
         const T t = fma(rv.x, rv.x, rv.y * rv.y);
         rr += t;
         corr = fma(w, t, corr);
       }
       if (G.nz > 1) {
         for (unsigned int q = wall_hi + t0; q < n / 2; q += stride) {
-          const V2 rv = update_pair<T, V2>(q, alpha, x, r, p, Ap);
+          const V2 rv = update_pair<T, V2>(q, alpha, r, Ap);
           const T t = fma(rv.x, rv.x, rv.y * rv.y);
           rr += t;
           corr = fma(w, t, corr);
@@ -446,7 +458,6 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x
   } else {
     // general walls: per-cell class
     for (unsigned int c = t0; c < n; c += stride) {
-      x[c] = fma(alpha, p[c], x[c]);
       const T rn = fma(-alpha, Ap[c], r[c]);
       r[c] = rn;
       rr = fma(rn, rn, rr);
@@ -459,10 +470,13 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ x
     finish_iteration(st, tot[0], tot[1], true);
 }
 
+// x += alpha p when x lags (before a residual replacement, a confirmation
+// and at the end of a solve).  With check, a finished solve returns at once.
 template <typename T>
-__global__ void __launch_bounds__(FNT) k_axpy2(const GeoL G, T *__restrict__ x, const T *__restrict__ p,
-                                               const DevState *st) {
-  if (*(volatile const int *)&st->done) return;
+__global__ void __launch_bounds__(FNT) k_settle(const GeoL G, T *__restrict__ x, const T *__restrict__ p,
+                                                const DevState *st, int check) {
+  if (check && *(volatile const int *)&st->done) return;
+  if (!*(volatile const int *)&st->dlag) return;
   const T alpha = (T)(*(volatile const double *)&st->alpha);
   const unsigned int n = (unsigned int)G.n;
   for (unsigned int c = blockIdx.x * FNT + threadIdx.x; c < n; c += gridDim.x * FNT) x[c] = fma(alpha, p[c], x[c]);
@@ -555,15 +569,18 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       st->rr = rr1;
       st->iter = 0;
       st->first = 1;
+      st->dlag = 0;
       st->replacements = 0;
       if (tot[2] < st->tiny) st->done = DONE_TINY;  // src/cuda_solver.cu:178-190
       else if (st->stop == 1 && rr1 <= st->tol2bb) st->done = DONE_CONVERGED;
       else st->done = RUNNING;
     } else if (mode == 1) {
       st->replacements += 1;
+      st->dlag = 0;  // x was settled before this residual
       finish_iteration(st, rz1, rr1, true);
     } else {  // confirm
       st->replacements += 1;
+      st->dlag = 0;
       st->rz_last = rz1;
       st->rr = rr1;
       if (rr1 <= st->tol2bb) {

@@ -47,6 +47,8 @@ struct GraphCache {
 struct IrBuffers;   // FP32 inner-sweep workspace (bbpp_ir.cu)
 struct NetWork;     // learned-guess workspace (bbpp_net.cu)
 
+struct bbpp_tma_state;
+
 struct bbpp_ctx {
   bbpp_grid grid{};
   bbpp::Geo G{};       // unscaled operator (kernel-level entry points, checks)
@@ -80,6 +82,7 @@ struct bbpp_ctx {
   std::string err;
   IrBuffers *ir = nullptr;
   NetWork *net = nullptr;
+  bbpp_tma_state *tma = nullptr;  // launch shape and tensor maps of the TMA search kernel
 };
 
 void bbpp_record_error(bbpp_ctx *ctx, cudaError_t e, const char *what, int line);
@@ -106,6 +109,12 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
 void bbpp_ir_free(bbpp_ctx *ctx);
 
 void bbpp_set_reliable(double *xhi, const double *rhs);
+// TMA-staged FP32 search kernel (bbpp_tma.cu)
+void bbpp_tma_init(bbpp_ctx *ctx);
+void bbpp_tma_free(bbpp_ctx *ctx);
+size_t bbpp_tma_partials(const bbpp_ctx *ctx);
+bool bbpp_tma_search(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const float *pold, float *pnew, float *Ap,
+                     float *x, bbpp::DevState *st);
 int bbpp_residual_async(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x, double *r);
 
 // learned initial guess (bbpp_net.cu)

@@ -83,10 +83,7 @@ static int solve_reliable(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs,
   rc = bbpp_pcg_loop<float>(ctx, mask, b->r, b->d, b->rd, p, b->Ap, st, hst, o->replace_every,
                             o->stop == BBPP_STOP_TRUE_REL, true, &it);
   bbpp_set_reliable(nullptr, nullptr);
-  if (rc) return rc;
-  k_add_correction<<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, x, b->d);
-  ctx->launches += 1;
-  CK(cudaGetLastError());
+  if (rc) return rc;  // the loop's last fold has brought x up to date
   rep->iters = it;
   rep->outer = hst->replacements;
   rep->replacements = hst->replacements;
@@ -96,12 +93,13 @@ static int solve_reliable(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs,
   switch (hst->done) {
     case DONE_CONVERGED: rep->status = BBPP_CONVERGED; break;
     case DONE_TINY: rep->status = BBPP_TINY_RHS; break;
+    case DONE_TIMEOUT: rep->status = BBPP_WAIT_TIMEOUT; break;
     case DONE_NAN: rep->status = BBPP_NAN; break;
     default: rep->status = BBPP_MAX_ITER;
   }
-  // bytes: 41 B/cell per FP32 iteration; each reliable update folds (12) and
-  // forms the FP64 residual (21); the initial residual and final fold likewise
-  rep->bytes = (double)n * (41.0 * it + 33.0 * (hst->replacements + 1));
+  // canonical bytes of the work (the reference formulation's traffic): 41
+  // B/cell per FP32 iteration, 25 per FP64 residual and 12 per fold
+  rep->bytes = (double)n * (41.0 * it + 37.0 * (hst->replacements + 1));
   return 0;
 }
 
@@ -195,6 +193,10 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
       status = BBPP_NAN;
       break;
     }
+    if (hsti->done == DONE_TIMEOUT) {
+      status = BBPP_WAIT_TIMEOUT;
+      break;
+    }
   }
   rep->iters = inner_total;
   rep->outer = outer;
@@ -202,8 +204,9 @@ int bbpp_solve_ir(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, double 
   rep->rz = rz;
   rep->rel_resid = bb > 0 ? std::sqrt(std::max(0.0, rr) / bb) : 0.0;
   rep->status = status;
-  // bytes: 41 B/cell per inner iteration (FP32 vectors), 25 B/cell per FP64
-  // outer residual (x, rhs, mask in; FP32 r out ~ 21) and 12 B per correction
+  // canonical bytes of the work (the reference formulation's traffic): 41
+  // B/cell per inner FP32 iteration, 25 per FP64 outer residual, 12 per
+  // correction
   rep->bytes = (double)n * (41.0 * inner_total + 25.0 * (outer + 1) + 12.0 * outer);
   return 0;
 }

@@ -236,7 +236,7 @@ static void stencil_shape(bbpp_ctx *ctx) {
     ctx->pgrid[prec] = dim3(fx, fy, nzf);
   }
   int per_sm2 = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k2_update<double>, FNT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_settle<double>, FNT, 0);
   if (per_sm2 < 1) per_sm2 = 1;
   long long eb = std::min<long long>((G.n + NT - 1) / NT, (long long)ctx->sms * per_sm2);
   ctx->egrid = (int)std::max<long long>(1, eb);
@@ -260,13 +260,14 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
   geol_init(ctx->G, &ctx->GL);
   ctx->sms = dev_sms();
   stencil_shape(ctx);
+  bbpp_tma_init(ctx);
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
       std::max<size_t>(std::max<size_t>((size_t)ctx->sgrid.x * ctx->sgrid.y * ctx->sgrid.z, (size_t)ctx->egrid),
                        (size_t)ctx->fgrid.x * ctx->fgrid.y * ctx->fgrid.z),
       std::max<size_t>(std::max<size_t>((size_t)ctx->pgrid[0].x * ctx->pgrid[0].y * ctx->pgrid[0].z,
                                         (size_t)ctx->pgrid[1].x * ctx->pgrid[1].y * ctx->pgrid[1].z),
-                       (size_t)((ctx->G.nx + 63) / 64) * ((ctx->G.ny + 7) / 8) * ctx->G.nz));
+                       bbpp_tma_partials(ctx)));
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   ctx->stream = ctx->own_stream;
@@ -305,6 +306,7 @@ extern "C" int bbpp_destroy(bbpp_ctx *ctx) {
   drop_graphs(ctx);
   bbpp_ir_free(ctx);
   bbpp_net_ctx_free(ctx);
+  bbpp_tma_free(ctx);
   if (ctx->st) cudaFree(ctx->st);
   if (ctx->partials) cudaFree(ctx->partials);
   if (ctx->r) cudaFree(ctx->r);
@@ -374,36 +376,38 @@ extern "C" const char *bbpp_version(void) { return "bbpp 0.1 (sm_103a)"; }
 // ---------------------------------------------------------------- launches --
 // All launches go to ctx->stream.  Typed on the vector element.
 template <typename T>
-static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap,
+static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap, T *x,
                                DevState *st) {
-  // bytes/cell: read r, p_old (+ mask), write p_new, Ap
-  bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_SEARCH_SPMV : KK_SEARCH_SPMV_F32, 4.0 * sizeof(T) + (mask ? 1 : 0));
+  // bytes/cell: read r, p_old (+ mask), write p_new, Ap; read and write x
+  bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_SEARCH_SPMV : KK_SEARCH_SPMV_F32, 6.0 * sizeof(T) + (mask ? 1 : 0));
   const int prec = sizeof(T) == 8 ? 1 : 0;
   cudaStream_t s = ctx->stream;
-  {
+  if (sizeof(T) == 4 && bbpp_tma_search(ctx, mask, (const float *)r, (const float *)pold, (float *)pnew,
+                                        (float *)Ap, (float *)x, st)) {
+    // FP32 on a TMA-eligible grid: launched by bbpp_tma_search
+  } else {
     const dim3 g = ctx->pgrid[prec];
     const int kz = ctx->pkz[prec];
     if (mask) {
       if (ctx->GL.iso)
-        k1_search2<T, true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+        k1_search2<T, true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
       else
-        k1_search2<T, true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+        k1_search2<T, true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
     } else {
       if (ctx->GL.iso)
-        k1_search2<T, false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+        k1_search2<T, false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
       else
-        k1_search2<T, false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, mask, st, ctx->partials, kz);
+        k1_search2<T, false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
     }
   }
   bbpp_rec_end(ctx);
 }
 
 template <typename T>
-static void launch_update(bbpp_ctx *ctx, T *x, T *r, const T *p, const T *Ap, DevState *st, bool rr) {
-  (void)rr;
-  // bytes/cell: read x, r, p, Ap, write x, r
-  bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_UPDATE : KK_UPDATE_F32, 6.0 * sizeof(T));
-  k2_update<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, r, p, Ap, st, ctx->partials);
+static void launch_update(bbpp_ctx *ctx, T *r, const T *Ap, DevState *st) {
+  // bytes/cell: read r, Ap, write r
+  bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_UPDATE : KK_UPDATE_F32, 3.0 * sizeof(T));
+  k2_update<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, r, Ap, st, ctx->partials);
   bbpp_rec_end(ctx);
 }
 
@@ -469,24 +473,43 @@ void bbpp_set_reliable(double *xhi, const double *rhs) {
   t_rel.rhs = rhs;
 }
 
-// x_hi += d; d = 0 (kernels of a finished solve return at once when check)
-__global__ void k_fold(const GeoL G, double *__restrict__ xhi, float *__restrict__ d, const DevState *st,
-                       int check) {
+// Reliable update of the mixed-precision solve: x_hi += d (+ alpha p when d
+// lags), d = 0, all in FP64.  With check, a finished solve returns at once.
+__global__ void __launch_bounds__(FNT) k_fold(const GeoL G, double *__restrict__ xhi, float *__restrict__ d,
+                                              const float *__restrict__ p, const DevState *st, int check) {
   if (check && *(volatile const int *)&st->done) return;
+  const bool lag = *(volatile const int *)&st->dlag;
+  const double alpha = lag ? *(volatile const double *)&st->alpha : 0.0;
   const unsigned int n = (unsigned int)G.n;
-  for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-    xhi[c] += (double)d[c];
+  for (unsigned int c = blockIdx.x * FNT + threadIdx.x; c < n; c += gridDim.x * FNT) {
+    double v = xhi[c] + (double)d[c];
+    if (lag) v = fma(alpha, (double)p[c], v);
+    xhi[c] = v;
     d[c] = 0.f;
   }
 }
 
-// the residual step of an iteration or a confirmation, for vectors of type T
+// x += alpha p if x lags (check: return at once in a finished solve)
 template <typename T>
-static void launch_replace(bbpp_ctx *ctx, const uint8_t *mask, T *x, const T *rhs, T *r, DevState *st, int mode) {
+static void launch_settle(bbpp_ctx *ctx, T *x, const T *p, DevState *st, int check) {
+  bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_AXPY : KK_AXPY_F32, 3.0 * sizeof(T));
+  k_settle<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, p, st, check);
+  bbpp_rec_end(ctx);
+}
+
+// The residual step of an iteration or a confirmation, for vectors of type T:
+// bring x up to date (p = the last search direction), then r from x.
+template <typename T>
+static void launch_replace(bbpp_ctx *ctx, const uint8_t *mask, T *x, const T *rhs, T *r, const T *p, DevState *st,
+                           int mode) {
+  const int check = mode == RES_ITER;
   if (sizeof(T) == 4 && t_rel.xhi) {
-    k_fold<<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, t_rel.xhi, (float *)x, st, mode == RES_ITER);
+    bbpp_rec_begin(ctx, KK_AXPY_F32, 20.0);
+    k_fold<<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, t_rel.xhi, (float *)x, (const float *)p, st, check);
+    bbpp_rec_end(ctx);
     bbpp_launch_resid_s<double, float>(ctx, mask, t_rel.xhi, t_rel.rhs, (float *)r, st, mode, ctx->GL.S);
   } else {
+    launch_settle<T>(ctx, x, p, st, check);
     bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, mode, t_bscale);
   }
 }
@@ -494,17 +517,12 @@ static void launch_replace(bbpp_ctx *ctx, const uint8_t *mask, T *x, const T *rh
 template <typename T>
 static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
                              DevState *st, int q, int replace_every, bool rr) {
+  (void)rr;
   // q = 1-based iteration number; K1 reads p[(q-1)%2] and writes p[q%2]
   T *pold = p[(q - 1) & 1], *pnew = p[q & 1];
-  launch_search_spmv<T>(ctx, mask, r, pold, pnew, Ap, st);
-  if (q % replace_every == 0) {
-    bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_AXPY : KK_AXPY_F32, 3.0 * sizeof(T));
-    k_axpy2<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, pnew, st);
-    bbpp_rec_end(ctx);
-    launch_replace<T>(ctx, mask, x, rhs, r, st, RES_ITER);
-  } else {
-    launch_update<T>(ctx, x, r, pnew, Ap, st, rr);
-  }
+  launch_search_spmv<T>(ctx, mask, r, pold, pnew, Ap, x, st);
+  if (q % replace_every == 0) launch_replace<T>(ctx, mask, x, rhs, r, pnew, st, RES_ITER);
+  else launch_update<T>(ctx, r, Ap, st);
 }
 
 // Capture (or reuse) the graph of iterations q0+1 .. q0+len for these buffers.
@@ -580,6 +598,7 @@ static int status_of(int done) {
     case DONE_MAX_ITER: return BBPP_MAX_ITER;
     case DONE_NAN: return BBPP_NAN;
     case DONE_TINY: return BBPP_TINY_RHS;
+    case DONE_TIMEOUT: return BBPP_WAIT_TIMEOUT;
     default: return BBPP_MAX_ITER;
   }
 }
@@ -620,7 +639,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
       for (int i = 1; i <= chunk; i++) {
         ctx->rec_iter = i;
         launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, q + i, replace_every, rr);
-        ctx->launches += ((q + i) % replace_every == 0) ? (t_rel.xhi ? 4 : 3) : 2;
+        ctx->launches += ((q + i) % replace_every == 0) ? 3 : 2;
       }
       ctx->rec = nullptr;
       CK(cudaGetLastError());
@@ -629,7 +648,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
       ctx->rec_iter = 1;
       launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, q + 1, replace_every, rr);
       ctx->rec = nullptr;
-      ctx->launches += ((q + 1) % replace_every == 0) ? (t_rel.xhi ? 4 : 3) : 2;
+      ctx->launches += ((q + 1) % replace_every == 0) ? 3 : 2;
       CK(cudaGetLastError());
     }
     CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
@@ -645,13 +664,22 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
         CK(cudaMemcpyAsync(&st->done, &hst->done, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
         break;
       }
-      launch_replace<T>(ctx, mask, x, rhs, r, st, RES_CONFIRM);
-      ctx->launches += (sizeof(T) == 4 && t_rel.xhi) ? 2 : 1;
+      launch_replace<T>(ctx, mask, x, rhs, r, p[q & 1], st, RES_CONFIRM);
+      ctx->launches += 2;
       CK(cudaGetLastError());
       CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
       CK(cudaStreamSynchronize(ctx->stream));
     }
   }
+  // x (or d) still lacks alpha p of the last iteration unless a residual
+  // replacement or confirmation came last
+  if (sizeof(T) == 4 && t_rel.xhi) {
+    k_fold<<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, t_rel.xhi, (float *)x, (const float *)p[q & 1], st, 0);
+  } else {
+    k_settle<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, p[q & 1], st, 0);
+  }
+  ctx->launches += 1;
+  CK(cudaGetLastError());
   if (iters_out) *iters_out = q;
   return 0;
 }
@@ -718,8 +746,9 @@ static int solve_fp64(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, dou
   rep->rz = hst->rz_last / S;  // back to the unscaled (r, z)
   rep->rel_resid = hst->bb > 0 ? std::sqrt(std::max(0.0, hst->rr) / hst->bb) / S : 0.0;
   rep->status = status_of(hst->done);
-  // algorithmic bytes: per iteration 81 (mask) or 80 B/cell; per replacement
-  // x-update 24 + residual 25; init residual 25
+  // canonical bytes of the work (the reference formulation's traffic): per
+  // iteration 81 (mask) or 80 B/cell; per replacement x-update 24 + residual
+  // 25; init residual 25
   const double n = (double)ctx->G.n;
   const double per_it = mask ? 81.0 : 80.0;
   rep->bytes = n * (per_it * iters + 49.0 * hst->replacements + 25.0);
@@ -810,6 +839,62 @@ extern "C" int bbpp_invm(bbpp_ctx *ctx, double *invM) {
   k_invm<<<ctx->egrid, NT, 0, ctx->stream>>>(ctx->G, invM);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+// One search-kernel launch on caller vectors (kernel-level checks).
+template <typename T>
+static int search_once(bbpp_ctx *ctx, int kernel, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap,
+                       T *x, DevState *st) {
+  if (kernel == 2) {
+    if (sizeof(T) != 4 || !bbpp_tma_search(ctx, mask, (const float *)r, (const float *)pold, (float *)pnew,
+                                           (float *)Ap, (float *)x, st))
+      return BBPP_BAD_ARG;
+  } else if (kernel == 1) {
+    const int prec = sizeof(T) == 8 ? 1 : 0;
+    const dim3 g = ctx->pgrid[prec];
+    const int kz = ctx->pkz[prec];
+    cudaStream_t s = ctx->stream;
+    if (mask) {
+      if (ctx->GL.iso) k1_search2<T, true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+      else k1_search2<T, true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+    } else {
+      if (ctx->GL.iso) k1_search2<T, false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+      else k1_search2<T, false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+    }
+  } else {
+    launch_search_spmv<T>(ctx, mask, r, pold, pnew, Ap, x, st);
+  }
+  return 0;
+}
+
+extern "C" int bbpp_search_step(bbpp_ctx *ctx, int precision, int kernel, const uint8_t *mask, const void *r,
+                                const void *pold, void *pnew, void *Ap, void *x, double beta, double alpha, int first,
+                                int lag, double *pAp) {
+  if (!ctx || !r || !pnew || !Ap || !x || (!first && !pold)) return BBPP_BAD_ARG;
+  if (precision != BBPP_FP64 && precision != BBPP_FP32_IR) return BBPP_BAD_ARG;
+  if (kernel < 0 || kernel > 2) return BBPP_BAD_ARG;
+  DevState *st = ctx->st + 1, *hst = ctx->hst + 1;
+  memset(hst, 0, sizeof(DevState));
+  hst->first = first ? 1 : 0;
+  hst->beta = beta;
+  hst->alpha = alpha;
+  hst->dlag = lag ? 1 : 0;
+  hst->rz = 1.0;  // the kernel leaves alpha = rz / (p, Ap)
+  CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
+  int rc;
+  if (precision == BBPP_FP64)
+    rc = search_once<double>(ctx, kernel, mask, (const double *)r, (const double *)pold, (double *)pnew,
+                             (double *)Ap, (double *)x, st);
+  else
+    rc = search_once<float>(ctx, kernel, mask, (const float *)r, (const float *)pold, (float *)pnew, (float *)Ap,
+                            (float *)x, st);
+  if (rc) return rc;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (hst->done == DONE_TIMEOUT) return BBPP_WAIT_TIMEOUT;
+  if (pAp) *pAp = hst->pAp;
   return 0;
 }
 

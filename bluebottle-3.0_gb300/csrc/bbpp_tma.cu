@@ -1,0 +1,511 @@
+// bbpp_tma.cu -- the FP32 search kernel with TMA-staged z-slabs.
+//
+// A CTA owns a slab of TY full x-rows (all nx cells of rows y0 .. y0+TY-1)
+// and marches through its z range.  For every plane one thread issues tensor
+// copies (cp.async.bulk.tensor) of r and p_old: the TY rows of the slab plus
+// the two halo rows y0-1 and y0+TY (wrapped for periodic y; a row outside a
+// wall reads the copy unit's zero fill).  Planes outside a Neumann wall are
+// zero-filled the same way.  The copies land in a ring of NS stages, each
+// completing on its own mbarrier, so several planes are in flight while the
+// CTA computes.  Because a stage holds whole rows, the x neighbours of the
+// periodic wrap are in shared memory already and no x halo is copied.
+//
+// Per plane: p_new = z + beta p_old over the stage (in place of r; z = r on
+// fluid cells away from walls, r / dL on wall classes), then, one plane
+// behind, Ap = L p_new on the slab's own cells with the (p, Ap) partial, the
+// stores of p_new and Ap, and x += alpha p_old (x lags one iteration).  The
+// arithmetic is the same as k1_search2's (apply_L), so both kernels give
+// bit-identical p_new, Ap and x.  Replaces PP_update_search + halo exchange +
+// PP_spmv_shared_load + thrust (p, Ap) (src/solver_kernel.cu:528-713,906-927,
+// src/cuda_solver.cu:201-205,256-263), in FP32.
+//
+// Every mbarrier wait is bounded (about one second of globaltimer); a wait
+// that runs out marks the CTA, which keeps to the barrier schedule, drains its
+// outstanding copies with bounded waits, and ends the solve with
+// DONE_TIMEOUT for the host to report.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <cstring>
+
+#include "bbpp_internal.h"
+#include "bbpp_fast.cuh"
+
+using namespace bbpp;
+
+namespace {
+
+constexpr int TNT = 256;  // threads per CTA
+
+__device__ __forceinline__ unsigned int smem_addr(const void *p) {
+  return (unsigned int)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned int bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned int parity) {
+  unsigned int ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for the phase with this parity; false after ~1 s without completion.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned int parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  for (unsigned int k = 1;; k++) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((k & 255u) == 0 && globaltimer() - t0 > 1000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, unsigned long long *bar, int c0,
+                                            int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
+      "[%2];" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(smem_addr(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, unsigned long long *bar, int c0,
+                                            int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, "
+      "%6}], [%2];" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(smem_addr(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+struct TmaMaps {
+  CUtensorMap r_rows, r_row, p_rows, p_row;  // TY-row and one-row boxes of r and p_old
+};
+
+// Load rows [y, y + nrow) of plane z of one array into dst (row-major, nx
+// floats per row).  4-D maps split x into 256-wide pieces (nx > 256).
+__device__ __forceinline__ void load_rows(float *dst, const CUtensorMap *map, unsigned long long *bar, int y, int z,
+                                          bool four_d) {
+  if (four_d) tma_load_4d(dst, map, bar, 0, 0, y, z);
+  else tma_load_3d(dst, map, bar, 0, y, z);
+}
+
+}  // namespace
+
+// NPT: float4 elements per thread per plane (TY * nx / 1024)
+template <int NPT, bool MASK, bool ISO>
+__global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constant__ TmaMaps M,
+                                              float *__restrict__ pnew, float *__restrict__ Ap,
+                                              float *__restrict__ x, const uint8_t *__restrict__ mask,
+                                              DevState *st, double *partials, int ty, int kz, int ns, int four_d) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ float s_dL[27], s_inv[27];
+  __shared__ double s_red[TNT / 32];
+  __shared__ unsigned long long s_full[8];
+  if (*(volatile int *)&st->done) return;
+  const bool first = *(volatile int *)&st->first;
+  const float beta = first ? 0.f : (float)(*(volatile double *)&st->beta);
+  const bool lag = !first && *(volatile int *)&st->dlag;
+  const float alpha = lag ? (float)(*(volatile double *)&st->alpha) : 0.f;
+  load_tabs<float>(G, s_dL, s_inv);
+
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const int nxv = nx >> 2;                 // float4 per row
+  const int rows = ty + 2;                 // stage rows with the halo
+  const int arr = rows * nx;               // floats per array per stage
+  float *stage = reinterpret_cast<float *>(smem_raw);  // [ns][2][rows][nx]
+  const int y0 = blockIdx.x * ty;
+  const int z0 = blockIdx.y * kz, z1 = min(z0 + kz, nz);
+  const int np = z1 - z0 + 2;              // planes z0-1 .. z1
+  const unsigned int plane = (unsigned int)nx * (unsigned int)ny;
+  const unsigned int tx_bytes = (unsigned int)((first ? 1 : 2) * arr * 4);
+  const int ys = G.py ? (y0 - 1 + ny) % ny : y0 - 1;  // south halo row (-1: zero fill)
+  const int yn = G.py ? (y0 + ty) % ny : y0 + ty;     // north halo row (ny: zero fill)
+
+  if (tid == 0) {
+    for (int s = 0; s < ns; s++) mbar_init(&s_full[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  auto issue = [&](int j) {  // thread 0: copies of plane z0-1+j into its stage
+    const int s = j % ns;
+    int zr = z0 - 1 + j;
+    if (G.pz) zr = (zr + nz) % nz;  // else -1 / nz read the zero fill
+    float *rs = stage + (size_t)s * 2 * arr;
+    unsigned long long *bar = &s_full[s];
+    mbar_expect_tx(bar, tx_bytes);
+    load_rows(rs + nx, &M.r_rows, bar, y0, zr, four_d);
+    load_rows(rs, &M.r_row, bar, ys, zr, four_d);
+    load_rows(rs + (ty + 1) * nx, &M.r_row, bar, yn, zr, four_d);
+    if (!first) {
+      float *ps = rs + arr;
+      load_rows(ps + nx, &M.p_rows, bar, y0, zr, four_d);
+      load_rows(ps, &M.p_row, bar, ys, zr, four_d);
+      load_rows(ps + (ty + 1) * nx, &M.p_row, bar, yn, zr, four_d);
+    }
+  };
+
+  bool bad = false;
+  // p_new over a stage, in place of r
+  auto prep = [&](int j) {
+    const int s = j % ns;
+    if (!mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u)) bad = true;
+    float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)s * 2 * arr);
+    const float4 *ps = reinterpret_cast<const float4 *>(stage + (size_t)s * 2 * arr + arr);
+    int zr = z0 - 1 + j;
+    const int gz = halo_index(zr, nz, G.pz);
+    const int wz = gz >= 0 ? 9 * wall_count(gz, nz, G.pz) : 0;
+    const int nel = rows * nxv;
+    if (G.px && G.py && wz == 0) {
+      for (int e = tid; e < nel; e += TNT) {
+        float4 v = rs[e];
+        if (!first) {
+          const float4 q = ps[e];
+          v.x = fmaf(beta, q.x, v.x);
+          v.y = fmaf(beta, q.y, v.y);
+          v.z = fmaf(beta, q.z, v.z);
+          v.w = fmaf(beta, q.w, v.w);
+        }
+        rs[e] = v;
+      }
+    } else {
+      for (int e = tid; e < nel; e += TNT) {
+        const int row = e / nxv, c4 = e - row * nxv;
+        const int gy = halo_index(y0 - 1 + row, ny, G.py);
+        const int wy = gy >= 0 ? 3 * wall_count(gy, ny, G.py) : 0;
+        const int xb = 4 * c4;
+        float4 v = rs[e];
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!first) q = ps[e];
+        float *vv = reinterpret_cast<float *>(&v);
+        const float *qq = reinterpret_cast<const float *>(&q);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int cls = wall_count(xb + i, nx, G.px) + wy + wz;
+          const float zv = cls ? vv[i] * s_inv[cls] : vv[i];
+          vv[i] = first ? zv : fmaf(beta, qq[i], zv);
+        }
+        rs[e] = v;
+      }
+    }
+  };
+
+  // own elements of this thread: float4 tid + k * TNT of the slab's TY x nxv
+  int orow[NPT], oc4[NPT];
+#pragma unroll
+  for (int k = 0; k < NPT; k++) {
+    const int e = tid + k * TNT;
+    orow[k] = e / nxv;
+    oc4[k] = e - orow[k] * nxv;
+  }
+  // own-cell mask and x of the next plane, loaded one plane ahead
+  uchar4 mk[NPT];
+  float4 xv[NPT];
+  auto fetch = [&](int zc) {
+#pragma unroll
+    for (int k = 0; k < NPT; k++) {
+      const int row = orow[k], c4 = oc4[k];
+      const unsigned int c = plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + row) + 4u * c4;
+      if (MASK) mk[k] = *reinterpret_cast<const uchar4 *>(mask + c);
+      if (lag) xv[k] = *reinterpret_cast<const float4 *>(x + c);
+    }
+  };
+
+  float acc = 0.f;
+  auto stencil = [&](int j) {
+    const int zc = z0 - 1 + j;
+    const float *cs = stage + (size_t)(j % ns) * 2 * arr;           // p_new, plane z
+    const float *ts = stage + (size_t)((j + 1) % ns) * 2 * arr;     // plane z+1
+    const float *bs = stage + (size_t)((j - 1 + ns) % ns) * 2 * arr;  // plane z-1
+    const float *po = cs + arr;                                      // p_old, plane z
+    const int wz = 9 * wall_count(zc, nz, G.pz);
+    const bool interior = G.px && G.py && wz == 0;
+#pragma unroll
+    for (int k = 0; k < NPT; k++) {
+      const int row = orow[k], c4 = oc4[k];
+      const int off = (row + 1) * nx + 4 * c4;
+      const float4 c = *reinterpret_cast<const float4 *>(cs + off);
+      const float4 n = *reinterpret_cast<const float4 *>(cs + off + nx);
+      const float4 s = *reinterpret_cast<const float4 *>(cs + off - nx);
+      const float4 t = *reinterpret_cast<const float4 *>(ts + off);
+      const float4 b = *reinterpret_cast<const float4 *>(bs + off);
+      // x neighbours: the adjacent lanes hold the adjacent float4 of the row
+      float w = __shfl_up_sync(0xffffffffu, c.w, 1);
+      float ea = __shfl_down_sync(0xffffffffu, c.x, 1);
+      if (lane == 0 || c4 == 0) {
+        const int xw = 4 * c4 - 1;
+        w = xw >= 0 ? cs[off - 1] : (G.px ? cs[(row + 1) * nx + nx - 1] : 0.f);
+      }
+      if (lane == 31 || c4 == nxv - 1) {
+        const int xe = 4 * c4 + 4;
+        ea = xe < nx ? cs[off + 4] : (G.px ? cs[(row + 1) * nx] : 0.f);
+      }
+      float a0, a1, a2, a3;
+      if (interior) {
+        a0 = apply_L<float, ISO>(G, s_dL, 0, c.x, c.y, w, n.x, s.x, t.x, b.x);
+        a1 = apply_L<float, ISO>(G, s_dL, 0, c.y, c.z, c.x, n.y, s.y, t.y, b.y);
+        a2 = apply_L<float, ISO>(G, s_dL, 0, c.z, c.w, c.y, n.z, s.z, t.z, b.z);
+        a3 = apply_L<float, ISO>(G, s_dL, 0, c.w, ea, c.z, n.w, s.w, t.w, b.w);
+      } else {
+        const int wy = 3 * wall_count(y0 + row, ny, G.py) + wz;
+        const int xb = 4 * c4;
+        a0 = apply_L<float, ISO>(G, s_dL, wall_count(xb, nx, G.px) + wy, c.x, c.y, w, n.x, s.x, t.x, b.x);
+        a1 = apply_L<float, ISO>(G, s_dL, wall_count(xb + 1, nx, G.px) + wy, c.y, c.z, c.x, n.y, s.y, t.y, b.y);
+        a2 = apply_L<float, ISO>(G, s_dL, wall_count(xb + 2, nx, G.px) + wy, c.z, c.w, c.y, n.z, s.z, t.z, b.z);
+        a3 = apply_L<float, ISO>(G, s_dL, wall_count(xb + 3, nx, G.px) + wy, c.w, ea, c.z, n.w, s.w, t.w, b.w);
+      }
+      if (MASK) {
+        if (mk[k].x) a0 = 0.f;
+        if (mk[k].y) a1 = 0.f;
+        if (mk[k].z) a2 = 0.f;
+        if (mk[k].w) a3 = 0.f;
+      }
+      acc = fmaf(c.x, a0, acc);
+      acc = fmaf(c.y, a1, acc);
+      acc = fmaf(c.z, a2, acc);
+      acc = fmaf(c.w, a3, acc);
+      const unsigned int g = plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + row) + 4u * c4;
+      *reinterpret_cast<float4 *>(Ap + g) = make_float4(a0, a1, a2, a3);
+      *reinterpret_cast<float4 *>(pnew + g) = c;
+      if (lag) {
+        const float4 q = *reinterpret_cast<const float4 *>(po + off);
+        float4 xo = xv[k];
+        xo.x = fmaf(alpha, q.x, xo.x);
+        xo.y = fmaf(alpha, q.y, xo.y);
+        xo.z = fmaf(alpha, q.z, xo.z);
+        xo.w = fmaf(alpha, q.w, xo.w);
+        *reinterpret_cast<float4 *>(x + g) = xo;
+      }
+    }
+  };
+
+  if (tid == 0) {
+    const int pre = min(ns, np);
+    for (int j = 0; j < pre; j++) issue(j);
+  }
+  fetch(z0);
+  prep(0);
+  prep(1);
+  for (int j = 1; j <= z1 - z0; j++) {
+    prep(j + 1);
+    fence_proxy_async();  // this thread's stage writes before later tensor copies
+    __syncthreads();
+    if (tid == 0 && j >= 2 && j - 2 + ns < np) issue(j - 2 + ns);
+    // the mask / x registers of plane j are consumed here, then refilled
+    stencil(j);
+    if (j < z1 - z0) fetch(z0 + j);
+  }
+
+  if (__syncthreads_or(bad)) {
+    // drain: every stage's last issued copy, with bounded waits
+    if (tid == 0) {
+      for (int j = max(0, np - ns); j < np; j++) mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u);
+      atomicExch(&st->done, (int)DONE_TIMEOUT);
+    }
+    return;
+  }
+  double v[1] = {(double)acc}, tot[1];
+  const unsigned int nb = gridDim.x * gridDim.y;
+  const unsigned int bid = blockIdx.x + gridDim.x * blockIdx.y;
+  if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
+    st->pAp = tot[0];
+    st->alpha = st->rz / tot[0];
+    st->first = 0;
+    st->dlag = 1;
+  }
+}
+
+// ------------------------------------------------------------------ host --
+namespace {
+
+typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  }
+  return fn;
+}
+
+// map of an nx x ny x nz float array with boxes of nrow full rows
+bool make_map(CUtensorMap *m, const float *base, int nx, int ny, int nz, int nrow) {
+  EncodeTiled fn = encode_fn();
+  if (!fn) return false;
+  CUresult r;
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  if (nx <= 256) {
+    const cuuint64_t dim[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t str[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)nx, (cuuint32_t)nrow, 1};
+    r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dim, str, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  } else {  // x split into 256-wide pieces so a box still lands as whole rows
+    const cuuint64_t dim[4] = {256, (cuuint64_t)(nx / 256), (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t str[3] = {1024, (cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    const cuuint32_t box[4] = {256, (cuuint32_t)(nx / 256), (cuuint32_t)nrow, 1};
+    r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(base), dim, str, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  }
+  return r == CUDA_SUCCESS;
+}
+
+struct MapPair {
+  const float *ptr;
+  CUtensorMap rows, row;
+};
+
+template <int NPT, bool MASK, bool ISO>
+void set_smem_attr(int bytes) {
+  cudaFuncSetAttribute(k1_tma<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+int env_int(const char *name, int dflt) {
+  const char *e = getenv(name);
+  return e ? atoi(e) : dflt;
+}
+
+}  // namespace
+
+struct bbpp_tma_state {
+  bool ok = false;
+  int ty = 0, npt = 0, ns = 0, kz = 0, four_d = 0, smem = 0;
+  dim3 grid;
+  std::vector<MapPair> maps;
+};
+
+// Decide whether the grid suits the TMA kernel and pick its launch shape.
+void bbpp_tma_init(bbpp_ctx *ctx) {
+  bbpp_tma_state *t = new bbpp_tma_state();
+  ctx->tma = t;
+  const GeoL &G = ctx->GL;
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  if (env_int("BBPP_TMA", 1) == 0) return;
+  if (!encode_fn()) return;
+  int ty;
+  if (nx <= 256 && nx % 32 == 0) ty = nx >= 256 ? 4 : 1024 / nx;
+  else if (nx % 256 == 0 && nx <= 1024) ty = 4;
+  else return;
+  if (ny % ty != 0 || ty > 256) return;
+  const int npt = ty * nx / 1024;
+  if (npt != 1 && npt != 2 && npt != 4) return;
+  const int stage = 2 * (ty + 2) * nx * 4;
+  int ns = env_int("BBPP_TMA_NS", 6);
+  ns = std::max(4, std::min(8, ns));  // >= 4: the refilled stage is never one of the three in use
+  while (ns > 4 && ns * stage > 200 * 1024) ns--;
+  if (ns * stage > 200 * 1024) return;
+  t->ty = ty;
+  t->npt = npt;
+  t->ns = ns;
+  t->smem = ns * stage;
+  t->four_d = nx > 256;
+  // one wave of resident CTAs
+  int per_sm = 0;
+#define BBPP_TMA_ATTR(N)                                                                          \
+  set_smem_attr<N, true, true>(t->smem);                                                          \
+  set_smem_attr<N, true, false>(t->smem);                                                         \
+  set_smem_attr<N, false, true>(t->smem);                                                         \
+  set_smem_attr<N, false, false>(t->smem);                                                        \
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k1_tma<N, true, true>, TNT, t->smem);
+  if (npt == 1) { BBPP_TMA_ATTR(1) }
+  else if (npt == 2) { BBPP_TMA_ATTR(2) }
+  else { BBPP_TMA_ATTR(4) }
+#undef BBPP_TMA_ATTR
+  cudaGetLastError();
+  if (per_sm < 1) return;
+  const int slabs = ny / ty;
+  const long long target = (long long)ctx->sms * per_sm;
+  int nzc = (int)std::max<long long>(1, target / slabs);
+  nzc = std::min(nzc, nz);
+  int kz = (nz + nzc - 1) / nzc;
+  nzc = (nz + kz - 1) / kz;
+  t->kz = kz;
+  t->grid = dim3(slabs, nzc, 1);
+  t->ok = true;
+}
+
+void bbpp_tma_free(bbpp_ctx *ctx) {
+  delete ctx->tma;
+  ctx->tma = nullptr;
+}
+
+size_t bbpp_tma_partials(const bbpp_ctx *ctx) {
+  return (ctx->tma && ctx->tma->ok) ? (size_t)ctx->tma->grid.x * ctx->tma->grid.y : 0;
+}
+
+static const MapPair *get_maps(bbpp_tma_state *t, const float *p, const GeoL &G) {
+  for (auto &m : t->maps)
+    if (m.ptr == p) return &m;
+  MapPair m;
+  m.ptr = p;
+  if (!make_map(&m.rows, p, G.nx, G.ny, G.nz, t->ty) || !make_map(&m.row, p, G.nx, G.ny, G.nz, 1)) return nullptr;
+  if (t->maps.size() >= 16) t->maps.erase(t->maps.begin());
+  t->maps.push_back(m);
+  return &t->maps.back();
+}
+
+bool bbpp_tma_search(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const float *pold, float *pnew, float *Ap,
+                     float *x, DevState *st) {
+  bbpp_tma_state *t = ctx->tma;
+  if (!t || !t->ok) return false;
+  const MapPair *mr = get_maps(t, r, ctx->GL);
+  const MapPair *mp = get_maps(t, pold, ctx->GL);
+  if (!mr || !mp) return false;
+  TmaMaps M;
+  M.r_rows = mr->rows;
+  M.r_row = mr->row;
+  M.p_rows = mp->rows;
+  M.p_row = mp->row;
+  cudaStream_t s = ctx->stream;
+#define BBPP_TMA_LAUNCH(N, MK, IS)                                                                        \
+  k1_tma<N, MK, IS><<<t->grid, TNT, t->smem, s>>>(ctx->GL, M, pnew, Ap, x, mask, st, ctx->partials, t->ty, \
+                                                  t->kz, t->ns, t->four_d)
+#define BBPP_TMA_NPT(N)                            \
+  if (mask) {                                      \
+    if (ctx->GL.iso) BBPP_TMA_LAUNCH(N, true, true);   \
+    else BBPP_TMA_LAUNCH(N, true, false);              \
+  } else {                                         \
+    if (ctx->GL.iso) BBPP_TMA_LAUNCH(N, false, true);  \
+    else BBPP_TMA_LAUNCH(N, false, false);             \
+  }
+  if (t->npt == 1) { BBPP_TMA_NPT(1) }
+  else if (t->npt == 2) { BBPP_TMA_NPT(2) }
+  else { BBPP_TMA_NPT(4) }
+#undef BBPP_TMA_NPT
+#undef BBPP_TMA_LAUNCH
+  return true;
+}

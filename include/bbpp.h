@@ -129,6 +129,15 @@ int bbpp_solve_host(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, doubl
 /* Kernel-level entry points (device pointers), used for parity checks. */
 int bbpp_spmv(bbpp_ctx *ctx, const uint8_t *mask, const double *p, double *Ap);
 int bbpp_invm(bbpp_ctx *ctx, double *invM);
+/* One launch of the PCG search kernel on caller vectors, on the scaled operator L = S(-A) with
+ * S = 1 / (2/dx^2 + 2/dy^2 + 2/dz^2) (kernel-level checks; no counterpart in the reference, whose
+ * PP_update_search + PP_spmv_shared_load + (p, Ap) in src/solver_kernel.cu:528-713,906-927 it fuses).
+ * precision BBPP_FP64 (double vectors) or BBPP_FP32_IR (float vectors); kernel 0 = the solver's
+ * choice, 1 = the z-marching tile kernel, 2 = the TMA-staged kernel (FP32 only; BBPP_BAD_ARG when the
+ * grid does not suit it).  p_new = z + beta p_old (first: p_new = z), z = r / diag(L); Ap = L p_new
+ * (0 on solid cells); x += alpha p_old when lag; *pAp = (p_new, Ap). */
+int bbpp_search_step(bbpp_ctx *ctx, int precision, int kernel, const uint8_t *mask, const void *r, const void *pold,
+                     void *pnew, void *Ap, void *x, double beta, double alpha, int first, int lag, double *pAp);
 /* Residual: r = rhs - (-A)x; also returns (r,r) and (rhs,rhs). */
 int bbpp_residual(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x,
                   double *r, double *rr, double *bb);
