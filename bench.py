@@ -237,6 +237,7 @@ def run_ours(args):
     net_info = None
     methods = {"fp64": dict(precision=bbpp.FP64), "ir": dict(precision=bbpp.FP32_IR),
                "ir_restart": dict(precision=bbpp.FP32_IR, ir_mode=bbpp.IR_RESTART),
+               "ir_every50": dict(precision=bbpp.FP32_IR, ir_drop=0.0),
                "ir_warm": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_GIVEN)}
     headline = "ir"
     if not args.no_learned and args.only in (None, "learned_ir"):
@@ -400,7 +401,7 @@ def main():
     ap.add_argument("--net", default=None, help="load (or save after training) the learned-guess network here")
     ap.add_argument("--train-samples", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=1500)
-    ap.add_argument("--only", default=None, choices=["fp64", "ir", "ir_restart", "ir_warm", "learned_ir"],
+    ap.add_argument("--only", default=None, choices=["fp64", "ir", "ir_restart", "ir_every50", "ir_warm", "learned_ir"],
                     help="run only warm-up + steps solves of one method (profiler runs)")
     ap.add_argument("--ref-iters", type=int, default=0,
                     help="iterations of a full solve for the reference arm (0: the measured C3 count)")

@@ -42,7 +42,24 @@ struct DevState {
   unsigned int ticket;  // arrival counter of the last-CTA reductions
   int dlag;        // x lacks alpha * p of the last search direction (added by the next search kernel)
   double tiny;     // (rhs,rhs) below this ends the solve at once (DONE_TINY)
+  // residual replacement at a checkpoint (every replace_every iterations)
+  // happens when rep_now; the search kernel sets it from rep_d2 (0: always;
+  // else once (r,r) <= rep_d2 * rr_ref, the (r,r) of the last replacement)
+  // or when rep_maxgap iterations have passed since the last one
+  double rr_ref;
+  double rep_d2;
+  int rep_maxgap;
+  int last_rep;
+  int rep_now;
+  int pad2;
 };
+
+// Set by the last CTA of a search kernel: does this iteration's checkpoint
+// (if it is one) replace the residual?
+__device__ __forceinline__ void decide_replacement(DevState *st) {
+  st->rep_now = (st->rep_d2 <= 0.0) || (st->rr <= st->rep_d2 * st->rr_ref) ||
+                (st->iter + 1 - st->last_rep >= st->rep_maxgap);
+}
 
 // Geometry and per-wall-class constants.  A cell's wall class is
 // wx + 3 wy + 9 wz where w_d counts the wall faces of the cell in direction d

@@ -379,6 +379,7 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
     st->alpha = st->rz / tot[0];
     st->first = 0;
     st->dlag = 1;
+    decide_replacement(st);
   }
 }
 
@@ -415,10 +416,11 @@ __device__ __forceinline__ V2 update_pair(unsigned int q, T alpha, T *__restrict
 // z-wall planes run in loops of their own with one weight each.
 template <typename T>
 __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r, const T *__restrict__ Ap,
-                                                 DevState *st, double *partials) {
+                                                 DevState *st, double *partials, int cond) {
   __shared__ T s_dL[27], s_inv[27];
   __shared__ double s_red[2 * FNT / 32];
   if (*(volatile int *)&st->done) return;
+  if (cond && *(volatile int *)&st->rep_now) return;  // a checkpoint that replaces the residual
   const T alpha = (T)(*(volatile double *)&st->alpha);
   load_tabs<T>(G, s_dL, s_inv);
   __syncthreads();
@@ -470,12 +472,20 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r
     finish_iteration(st, tot[0], tot[1], true);
 }
 
+// check: 0 always runs; 1 returns in a finished solve; 2 also returns at a
+// checkpoint that keeps the recursive residual
+__device__ __forceinline__ bool skip_step(const DevState *st, int check) {
+  if (!check) return false;
+  if (*(volatile const int *)&st->done) return true;
+  return check == 2 && !*(volatile const int *)&st->rep_now;
+}
+
 // x += alpha p when x lags (before a residual replacement, a confirmation
-// and at the end of a solve).  With check, a finished solve returns at once.
+// and at the end of a solve).
 template <typename T>
 __global__ void __launch_bounds__(FNT) k_settle(const GeoL G, T *__restrict__ x, const T *__restrict__ p,
                                                 const DevState *st, int check) {
-  if (check && *(volatile const int *)&st->done) return;
+  if (skip_step(st, check)) return;
   if (!*(volatile const int *)&st->dlag) return;
   const T alpha = (T)(*(volatile const double *)&st->alpha);
   const unsigned int n = (unsigned int)G.n;
@@ -494,7 +504,7 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
   __shared__ TXT sp[3][FHY][FHX];
   __shared__ uint8_t sm[3][FHY][FHX + 2];
   __shared__ double s_red[3 * FNT / 32];
-  if (mode == 1 && *(volatile int *)&st->done) return;
+  if (mode == 1 && skip_step(st, 2)) return;
   load_tabs<TXT>(G, s_dL, s_inv);
   const int tid = threadIdx.x;
   const int tx = tid & 31, ty = tid >> 5;
@@ -571,6 +581,9 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       st->first = 1;
       st->dlag = 0;
       st->replacements = 0;
+      st->rr_ref = rr1;
+      st->last_rep = 0;
+      st->rep_now = 0;
       if (tot[2] < st->tiny) st->done = DONE_TINY;  // src/cuda_solver.cu:178-190
       else if (st->stop == 1 && rr1 <= st->tol2bb) st->done = DONE_CONVERGED;
       else st->done = RUNNING;
@@ -578,9 +591,13 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       st->replacements += 1;
       st->dlag = 0;  // x was settled before this residual
       finish_iteration(st, rz1, rr1, true);
+      st->rr_ref = rr1;
+      st->last_rep = st->iter;
     } else {  // confirm
       st->replacements += 1;
       st->dlag = 0;
+      st->rr_ref = rr1;
+      st->last_rep = st->iter;
       st->rz_last = rz1;
       st->rr = rr1;
       if (rr1 <= st->tol2bb) {

@@ -69,6 +69,8 @@ static int solve_reliable(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs,
   memset(hst, 0, sizeof(DevState));
   hst->tol2bb = o->tol * o->tol * (o->stop == 0 ? S : S * S);
   hst->tiny = 1e-16;
+  hst->rep_d2 = o->ir_drop * o->ir_drop;
+  hst->rep_maxgap = 8 * o->replace_every;
   hst->max_iter = o->max_iter;
   hst->stop = o->stop;
   hst->first = 1;

@@ -173,93 +173,129 @@ __global__ void k_prep(const T *__restrict__ rhs, const T *__restrict__ prev, co
   }
 }
 
+// The resampling kernels move 8 channels (16 bytes) per thread: C, the row
+// strides and the channel offsets are multiples of 8.  Voxel indices are
+// 32-bit (a batch holds fewer than 2^32 / 8 voxels).
+__device__ __forceinline__ void bf8_unpack(const uint4 u, float (&f)[8]) {
+  const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float2 t = __bfloat1622float2(h[i]);
+    f[2 * i] = t.x;
+    f[2 * i + 1] = t.y;
+  }
+}
+
+__device__ __forceinline__ uint4 bf8_pack(const float (&f)[8]) {
+  uint4 u;
+  __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; i++) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+  return u;
+}
+
+// voxel index of child q (0..7) of the half-resolution voxel (x, y, z) of batch b
+__device__ __forceinline__ unsigned int child_voxel(unsigned int b, unsigned int x, unsigned int y, unsigned int z,
+                                                    int q, unsigned int nx, unsigned int ny, unsigned int nz) {
+  return ((b * nz + 2 * z + (q >> 2)) * ny + 2 * y + ((q >> 1) & 1)) * nx + 2 * x + (q & 1);
+}
+
 // average pool 2x2x2: out[V/8][C] (ld C) from in (ld, off)
 __global__ void k_pool_fwd(const bf16 *__restrict__ in, int ldi, int off, int C, int nx, int ny, int nz, int nb,
                            bf16 *__restrict__ out) {
-  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-  const long long n = (long long)hx * hy * hz * nb * C;
-  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
-    const int c = (int)(e % C);
-    long long v = e / C;
-    const int x = (int)(v % hx);
+  const unsigned int hx = nx / 2, hy = ny / 2, hz = nz / 2, cv = C / 8;
+  const unsigned int n = hx * hy * hz * (unsigned int)nb * cv;
+  for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < n; e += gridDim.x * 256u) {
+    const unsigned int k = e % cv;
+    unsigned int v = e / cv;
+    const unsigned int x = v % hx;
     v /= hx;
-    const int y = (int)(v % hy);
+    const unsigned int y = v % hy;
     v /= hy;
-    const int z = (int)(v % hz);
-    const int b = (int)(v / hz);
-    float s = 0.f;
+    const unsigned int z = v % hz, b = v / hz;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-      const long long src = (long long)b * nx * ny * nz + ((long long)(2 * z + (q >> 2)) * ny + 2 * y + ((q >> 1) & 1)) * nx +
-                            2 * x + (q & 1);
-      s += __bfloat162float(in[src * ldi + off + c]);
+      const unsigned int src = child_voxel(b, x, y, z, q, nx, ny, nz);
+      float f[8];
+      bf8_unpack(*reinterpret_cast<const uint4 *>(in + (size_t)src * ldi + off + 8 * k), f);
+#pragma unroll
+      for (int i = 0; i < 8; i++) s[i] += f[i];
     }
-    out[e] = __float2bfloat16_rn(0.125f * s);
+#pragma unroll
+    for (int i = 0; i < 8; i++) s[i] *= 0.125f;
+    reinterpret_cast<uint4 *>(out)[e] = bf8_pack(s);
   }
 }
 
 // din[v][c] (ld C) = dskip[v][c] (ld, off; may be null) + dout[parent][c] / 8
 __global__ void k_pool_bwd(const bf16 *__restrict__ dout, const bf16 *__restrict__ dskip, int lds, int offs, int C,
                            int nx, int ny, int nz, int nb, bf16 *__restrict__ din) {
-  const long long n = (long long)nx * ny * nz * nb * C;
-  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
-    const int c = (int)(e % C);
-    long long v = e / C;
-    const int x = (int)(v % nx);
-    long long t = v / nx;
-    const int y = (int)(t % ny);
+  const unsigned int hx = nx / 2, hy = ny / 2, hz = nz / 2, cv = C / 8;
+  const unsigned int n = (unsigned int)nx * ny * nz * nb * cv;
+  for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < n; e += gridDim.x * 256u) {
+    const unsigned int k = e % cv;
+    const unsigned int v = e / cv;
+    const unsigned int x = v % nx;
+    unsigned int t = v / nx;
+    const unsigned int y = t % ny;
     t /= ny;
-    const int z = (int)(t % nz);
-    const int b = (int)(t / nz);
-    const long long par = (((long long)b * hz + z / 2) * hy + y / 2) * hx + x / 2;
-    float g = 0.125f * __bfloat162float(dout[par * C + c]);
-    if (dskip) g += __bfloat162float(dskip[v * lds + offs + c]);
-    din[e] = __float2bfloat16_rn(g);
+    const unsigned int z = t % nz, b = t / nz;
+    const unsigned int par = ((b * hz + z / 2) * hy + y / 2) * hx + x / 2;
+    float g[8], d[8];
+    bf8_unpack(reinterpret_cast<const uint4 *>(dout)[par * cv + k], g);
+#pragma unroll
+    for (int i = 0; i < 8; i++) g[i] *= 0.125f;
+    if (dskip) {
+      bf8_unpack(*reinterpret_cast<const uint4 *>(dskip + (size_t)v * lds + offs + 8 * k), d);
+#pragma unroll
+      for (int i = 0; i < 8; i++) g[i] += d[i];
+    }
+    reinterpret_cast<uint4 *>(din)[e] = bf8_pack(g);
   }
 }
 
 // nearest upsample x2: out[v][off + c] (ld) = in[parent][c] (ld C)
 __global__ void k_up_fwd(const bf16 *__restrict__ in, int C, int nx, int ny, int nz, int nb, bf16 *__restrict__ out,
                          int ldo, int off) {
-  const long long n = (long long)nx * ny * nz * nb * C;
-  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
-    const int c = (int)(e % C);
-    long long v = e / C;
-    const int x = (int)(v % nx);
-    long long t = v / nx;
-    const int y = (int)(t % ny);
+  const unsigned int hx = nx / 2, hy = ny / 2, hz = nz / 2, cv = C / 8;
+  const unsigned int n = (unsigned int)nx * ny * nz * nb * cv;
+  for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < n; e += gridDim.x * 256u) {
+    const unsigned int k = e % cv;
+    const unsigned int v = e / cv;
+    const unsigned int x = v % nx;
+    unsigned int t = v / nx;
+    const unsigned int y = t % ny;
     t /= ny;
-    const int z = (int)(t % nz);
-    const int b = (int)(t / nz);
-    const long long par = (((long long)b * hz + z / 2) * hy + y / 2) * hx + x / 2;
-    out[v * ldo + off + c] = in[par * C + c];
+    const unsigned int z = t % nz, b = t / nz;
+    const unsigned int par = ((b * hz + z / 2) * hy + y / 2) * hx + x / 2;
+    *reinterpret_cast<uint4 *>(out + (size_t)v * ldo + off + 8 * k) = reinterpret_cast<const uint4 *>(in)[par * cv + k];
   }
 }
 
 // din[p][c] (ld C, at half resolution) = sum of the 8 children dout[v][off + c]
 __global__ void k_up_bwd(const bf16 *__restrict__ dout, int ldo, int off, int C, int nx, int ny, int nz, int nb,
                          bf16 *__restrict__ din) {
-  const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-  const long long n = (long long)hx * hy * hz * nb * C;
-  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < n; e += (long long)gridDim.x * 256) {
-    const int c = (int)(e % C);
-    long long v = e / C;
-    const int x = (int)(v % hx);
+  const unsigned int hx = nx / 2, hy = ny / 2, hz = nz / 2, cv = C / 8;
+  const unsigned int n = hx * hy * hz * (unsigned int)nb * cv;
+  for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < n; e += gridDim.x * 256u) {
+    const unsigned int k = e % cv;
+    unsigned int v = e / cv;
+    const unsigned int x = v % hx;
     v /= hx;
-    const int y = (int)(v % hy);
+    const unsigned int y = v % hy;
     v /= hy;
-    const int z = (int)(v % hz);
-    const int b = (int)(v / hz);
-    float s = 0.f;
+    const unsigned int z = v % hz, b = v / hz;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-      const long long ch = (long long)b * nx * ny * nz + ((long long)(2 * z + (q >> 2)) * ny + 2 * y + ((q >> 1) & 1)) * nx +
-                           2 * x + (q & 1);
-      s += __bfloat162float(dout[ch * ldo + off + c]);
+      const unsigned int ch = child_voxel(b, x, y, z, q, nx, ny, nz);
+      float f[8];
+      bf8_unpack(*reinterpret_cast<const uint4 *>(dout + (size_t)ch * ldo + off + 8 * k), f);
+#pragma unroll
+      for (int i = 0; i < 8; i++) s[i] += f[i];
     }
-    din[e] = __float2bfloat16_rn(s);
+    reinterpret_cast<uint4 *>(din)[e] = bf8_pack(s);
   }
 }
 

@@ -348,6 +348,7 @@ extern "C" void bbpp_default_opts(bbpp_opts *o) {
   o->inner_tol = 1e-4;
   o->max_outer = 30;
   o->ir_mode = BBPP_IR_RELIABLE;
+  o->ir_drop = 1e-2;
   o->net = nullptr;
   o->prev = nullptr;
 }
@@ -403,11 +404,12 @@ static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, c
   bbpp_rec_end(ctx);
 }
 
+// cond: a checkpoint, where the update runs only if the residual is not replaced
 template <typename T>
-static void launch_update(bbpp_ctx *ctx, T *r, const T *Ap, DevState *st) {
+static void launch_update(bbpp_ctx *ctx, T *r, const T *Ap, DevState *st, int cond) {
   // bytes/cell: read r, Ap, write r
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_UPDATE : KK_UPDATE_F32, 3.0 * sizeof(T));
-  k2_update<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, r, Ap, st, ctx->partials);
+  k2_update<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, r, Ap, st, ctx->partials, cond);
   bbpp_rec_end(ctx);
 }
 
@@ -474,10 +476,10 @@ void bbpp_set_reliable(double *xhi, const double *rhs) {
 }
 
 // Reliable update of the mixed-precision solve: x_hi += d (+ alpha p when d
-// lags), d = 0, all in FP64.  With check, a finished solve returns at once.
+// lags), d = 0, all in FP64.  check as for k_settle.
 __global__ void __launch_bounds__(FNT) k_fold(const GeoL G, double *__restrict__ xhi, float *__restrict__ d,
                                               const float *__restrict__ p, const DevState *st, int check) {
-  if (check && *(volatile const int *)&st->done) return;
+  if (skip_step(st, check)) return;
   const bool lag = *(volatile const int *)&st->dlag;
   const double alpha = lag ? *(volatile const double *)&st->alpha : 0.0;
   const unsigned int n = (unsigned int)G.n;
@@ -502,7 +504,7 @@ static void launch_settle(bbpp_ctx *ctx, T *x, const T *p, DevState *st, int che
 template <typename T>
 static void launch_replace(bbpp_ctx *ctx, const uint8_t *mask, T *x, const T *rhs, T *r, const T *p, DevState *st,
                            int mode) {
-  const int check = mode == RES_ITER;
+  const int check = mode == RES_ITER ? 2 : 0;
   if (sizeof(T) == 4 && t_rel.xhi) {
     bbpp_rec_begin(ctx, KK_AXPY_F32, 20.0);
     k_fold<<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, t_rel.xhi, (float *)x, (const float *)p, st, check);
@@ -521,8 +523,14 @@ static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T
   // q = 1-based iteration number; K1 reads p[(q-1)%2] and writes p[q%2]
   T *pold = p[(q - 1) & 1], *pnew = p[q & 1];
   launch_search_spmv<T>(ctx, mask, r, pold, pnew, Ap, x, st);
-  if (q % replace_every == 0) launch_replace<T>(ctx, mask, x, rhs, r, pnew, st, RES_ITER);
-  else launch_update<T>(ctx, r, Ap, st);
+  if (q % replace_every == 0) {
+    // checkpoint: the search kernel has decided between the recursive update
+    // and a residual replacement; the other kernels return at once
+    launch_update<T>(ctx, r, Ap, st, 1);
+    launch_replace<T>(ctx, mask, x, rhs, r, pnew, st, RES_ITER);
+  } else {
+    launch_update<T>(ctx, r, Ap, st, 0);
+  }
 }
 
 // Capture (or reuse) the graph of iterations q0+1 .. q0+len for these buffers.
@@ -639,7 +647,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
       for (int i = 1; i <= chunk; i++) {
         ctx->rec_iter = i;
         launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, q + i, replace_every, rr);
-        ctx->launches += ((q + i) % replace_every == 0) ? 3 : 2;
+        ctx->launches += ((q + i) % replace_every == 0) ? 4 : 2;
       }
       ctx->rec = nullptr;
       CK(cudaGetLastError());
@@ -648,7 +656,7 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
       ctx->rec_iter = 1;
       launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, q + 1, replace_every, rr);
       ctx->rec = nullptr;
-      ctx->launches += ((q + 1) % replace_every == 0) ? 3 : 2;
+      ctx->launches += ((q + 1) % replace_every == 0) ? 4 : 2;
       CK(cudaGetLastError());
     }
     CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
@@ -724,6 +732,7 @@ static int check_opts(const bbpp_opts *o) {
   if (o->guess < BBPP_GUESS_ZERO || o->guess > BBPP_GUESS_LEARNED) return BBPP_BAD_ARG;
   if (o->stop != BBPP_STOP_REF_RZ && o->stop != BBPP_STOP_TRUE_REL) return BBPP_BAD_ARG;
   if (o->ir_mode != BBPP_IR_RELIABLE && o->ir_mode != BBPP_IR_RESTART) return BBPP_BAD_ARG;
+  if (!(o->ir_drop >= 0.0 && o->ir_drop < 1.0)) return BBPP_BAD_ARG;
   if (!(o->tol >= 0) || o->max_iter < 0 || o->replace_every < 1) return BBPP_BAD_ARG;
   if (o->guess == BBPP_GUESS_LEARNED && !o->net) return BBPP_BAD_ARG;
   return 0;

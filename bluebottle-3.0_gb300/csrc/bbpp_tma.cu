@@ -335,6 +335,7 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
     st->alpha = st->rz / tot[0];
     st->first = 0;
     st->dlag = 1;
+    decide_replacement(st);
   }
 }
 

@@ -90,6 +90,9 @@ typedef struct bbpp_opts {
   void *net;          /* GUESS_LEARNED: a bbpp_net handle */
   const double *prev; /* GUESS_LEARNED: previous pressure (device), may be NULL */
   int ir_mode;        /* FP32_IR: bbpp_ir_mode */
+  double ir_drop;     /* FP32_IR reliable mode: a checkpoint (every replace_every iterations) replaces the
+                         residual once ||r|| has dropped by this factor since the last replacement (and at
+                         least every 8 checkpoints); 0 = at every checkpoint.  Default 1e-2. */
 } bbpp_opts;
 
 typedef struct bbpp_report {

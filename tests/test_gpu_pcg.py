@@ -195,5 +195,9 @@ def test_solve_odd_shapes(lib, orc, dims, bc, precision, ir_mode):
     assert rep.status == bbpp.CONVERGED and rep.true_rel <= tol * 1.01
     xo, res = orc.pcg(to_orc(orc, g), b, mask, tol=1e-13)
     assert np.all(x[mask == 1] == 0)
+    if not mask.any():
+        # no solid cell: periodic/Neumann Poisson is singular and the solution
+        # is defined up to a constant, which FP32 round-off may shift
+        x, xo = x - x.mean(), xo - xo.mean()
     err = np.abs(x - xo).max() / max(np.abs(xo).max(), 1e-300)
     assert err < 1e4 * tol, err
