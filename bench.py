@@ -13,6 +13,7 @@ timed beside it.  The metric is solves/s (higher is better).
 oracle, OpenMP on all host cores) on a bounded sample of the same workload.
 """
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -391,6 +392,7 @@ def run_ours(args):
 
 
 def main():
+    faulthandler.enable()  # a crash in native code prints the Python stack
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)

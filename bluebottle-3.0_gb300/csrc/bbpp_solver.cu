@@ -534,6 +534,7 @@ static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T
 }
 
 // Capture (or reuse) the graph of iterations q0+1 .. q0+len for these buffers.
+// Returns its index in ctx->graphs, or -1 after a CUDA error.
 template <typename T>
 static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
                            DevState *st, int len, int replace_every, bool rr, cudaGraphExec_t *out) {
@@ -564,7 +565,7 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) {
     bbpp_record_error(c, e, "cudaStreamBeginCapture", __LINE__);
-    return BBPP_CUDA_ERROR;
+    return -1;
   }
   GraphCache gc;
   gc.key = key;
@@ -577,7 +578,7 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   e = cudaStreamEndCapture(ctx->stream, &graph);
   if (e != cudaSuccess) {
     bbpp_record_error(c, e, "cudaStreamEndCapture", __LINE__);
-    return BBPP_CUDA_ERROR;
+    return -1;
   }
   cudaGraphExec_t exec = nullptr;
   size_t nnodes = 0;
@@ -586,7 +587,7 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
     bbpp_record_error(c, e, "cudaGraphInstantiate", __LINE__);
-    return BBPP_CUDA_ERROR;
+    return -1;
   }
   if (ctx->graphs.size() >= 8) {
     cudaGraphExecDestroy(ctx->graphs.front().exec);

@@ -390,9 +390,14 @@ struct MapPair {
   CUtensorMap rows, row;
 };
 
+// Dynamic shared memory of one launch never exceeds this; the attribute is a
+// per-function cap shared by all contexts, so it is set once to the maximum
+// (a context of another grid must not lower it under this one).
+constexpr int kMaxStageBytes = 200 * 1024;
+
 template <int NPT, bool MASK, bool ISO>
-void set_smem_attr(int bytes) {
-  cudaFuncSetAttribute(k1_tma<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+void set_smem_attr() {
+  cudaFuncSetAttribute(k1_tma<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes);
 }
 
 int env_int(const char *name, int dflt) {
@@ -427,8 +432,8 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
   const int stage = 2 * (ty + 2) * nx * 4;
   int ns = env_int("BBPP_TMA_NS", 6);
   ns = std::max(4, std::min(8, ns));  // >= 4: the refilled stage is never one of the three in use
-  while (ns > 4 && ns * stage > 200 * 1024) ns--;
-  if (ns * stage > 200 * 1024) return;
+  while (ns > 4 && ns * stage > kMaxStageBytes) ns--;
+  if (ns * stage > kMaxStageBytes) return;
   t->ty = ty;
   t->npt = npt;
   t->ns = ns;
@@ -436,11 +441,25 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
   t->four_d = nx > 256;
   // one wave of resident CTAs
   int per_sm = 0;
-#define BBPP_TMA_ATTR(N)                                                                          \
-  set_smem_attr<N, true, true>(t->smem);                                                          \
-  set_smem_attr<N, true, false>(t->smem);                                                         \
-  set_smem_attr<N, false, true>(t->smem);                                                         \
-  set_smem_attr<N, false, false>(t->smem);                                                        \
+  static unsigned long long attr_set = 0;  // per device
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !(attr_set & (1ull << dev))) {
+    attr_set |= 1ull << dev;
+    set_smem_attr<1, true, true>();
+    set_smem_attr<1, true, false>();
+    set_smem_attr<1, false, true>();
+    set_smem_attr<1, false, false>();
+    set_smem_attr<2, true, true>();
+    set_smem_attr<2, true, false>();
+    set_smem_attr<2, false, true>();
+    set_smem_attr<2, false, false>();
+    set_smem_attr<4, true, true>();
+    set_smem_attr<4, true, false>();
+    set_smem_attr<4, false, true>();
+    set_smem_attr<4, false, false>();
+  }
+#define BBPP_TMA_ATTR(N) \
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k1_tma<N, true, true>, TNT, t->smem);
   if (npt == 1) { BBPP_TMA_ATTR(1) }
   else if (npt == 2) { BBPP_TMA_ATTR(2) }
@@ -468,29 +487,33 @@ size_t bbpp_tma_partials(const bbpp_ctx *ctx) {
   return (ctx->tma && ctx->tma->ok) ? (size_t)ctx->tma->grid.x * ctx->tma->grid.y : 0;
 }
 
-static const MapPair *get_maps(bbpp_tma_state *t, const float *p, const GeoL &G) {
-  for (auto &m : t->maps)
-    if (m.ptr == p) return &m;
+// tensor maps of one vector (copied out: the cache may reallocate)
+static bool get_maps(bbpp_tma_state *t, const float *p, const GeoL &G, MapPair *out) {
+  for (const auto &m : t->maps)
+    if (m.ptr == p) {
+      *out = m;
+      return true;
+    }
   MapPair m;
   m.ptr = p;
-  if (!make_map(&m.rows, p, G.nx, G.ny, G.nz, t->ty) || !make_map(&m.row, p, G.nx, G.ny, G.nz, 1)) return nullptr;
+  if (!make_map(&m.rows, p, G.nx, G.ny, G.nz, t->ty) || !make_map(&m.row, p, G.nx, G.ny, G.nz, 1)) return false;
   if (t->maps.size() >= 16) t->maps.erase(t->maps.begin());
   t->maps.push_back(m);
-  return &t->maps.back();
+  *out = m;
+  return true;
 }
 
 bool bbpp_tma_search(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const float *pold, float *pnew, float *Ap,
                      float *x, DevState *st) {
   bbpp_tma_state *t = ctx->tma;
   if (!t || !t->ok) return false;
-  const MapPair *mr = get_maps(t, r, ctx->GL);
-  const MapPair *mp = get_maps(t, pold, ctx->GL);
-  if (!mr || !mp) return false;
+  MapPair mr, mp;
+  if (!get_maps(t, r, ctx->GL, &mr) || !get_maps(t, pold, ctx->GL, &mp)) return false;
   TmaMaps M;
-  M.r_rows = mr->rows;
-  M.r_row = mr->row;
-  M.p_rows = mp->rows;
-  M.p_row = mp->row;
+  M.r_rows = mr.rows;
+  M.r_row = mr.row;
+  M.p_rows = mp.rows;
+  M.p_row = mp.row;
   cudaStream_t s = ctx->stream;
 #define BBPP_TMA_LAUNCH(N, MK, IS)                                                                        \
   k1_tma<N, MK, IS><<<t->grid, TNT, t->smem, s>>>(ctx->GL, M, pnew, Ap, x, mask, st, ctx->partials, t->ty, \

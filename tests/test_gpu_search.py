@@ -110,3 +110,25 @@ def test_fp64_search_matches_oracle(bbpp_lib, orc, dims, bc):
     assert np.abs(dap.download() - Aref).max() <= 1e-13 * np.abs(Aref).max()
     assert np.abs(dx.download() - (x + alpha * po)).max() <= 1e-15 * np.abs(x + alpha * po).max()
     assert abs(pAp - float(np.dot(pn.ravel(), dap.download().ravel()))) <= 1e-12 * abs(pAp)
+
+
+def test_contexts_of_different_grids(bbpp_lib):
+    """A context made later for another grid (a smaller TMA stage) leaves an
+    earlier context's FP32 solves working."""
+    ga = bbpp.Grid.make(128, 16, 16, 1 / 128, 1 / 16, 1 / 16, (P, P, P, P, N, N))
+    sa = bbpp.Solver(ga)
+    gb = bbpp.Grid.make(32, 32, 8, 1 / 32, 1 / 32, 1 / 8, (P,) * 6)
+    sb = bbpp.Solver(gb)
+    rng = np.random.default_rng(5)
+    mask = (rng.random(ga.shape) < 0.05).astype(np.uint8)
+    b = rng.uniform(-1, 1, ga.shape)
+    b[mask == 1] = 0
+    b[mask == 0] -= b[mask == 0].mean()
+    x, rep = sa.solve_host(b, mask, tol=1e-8, precision=bbpp.FP32_IR)
+    assert rep.status == bbpp.CONVERGED and rep.true_rel <= 1e-8 * 1.01
+    mb = np.zeros(gb.shape, np.uint8)
+    mb[0, 0, 0] = 1
+    bb = rng.uniform(-1, 1, gb.shape)
+    bb[mb == 1] = 0
+    xb, repb = sb.solve_host(bb, mb, tol=1e-8, precision=bbpp.FP32_IR)
+    assert repb.status == bbpp.CONVERGED
