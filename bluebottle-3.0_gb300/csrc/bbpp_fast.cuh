@@ -17,8 +17,8 @@
 //  k1_search2 p = invM r + beta p_old on a 64x16 tile plus halo (two cells per
 //             thread), ring of three planes in shared memory while the CTA
 //             marches in z; Ap = L p and the (p, Ap) partial.
-//  k2_update  x += alpha p, r -= alpha Ap, (r,r) and the wall correction of
-//             (r,z), vector loads.
+//  k2_update  r -= alpha Ap, (r,r) and the wall correction of (r,z), 16-byte
+//             vector loads.
 //  k_resid_s  r = bscale rhs - L x (solid cells 0) with (r,z), (r,r), (rhs,rhs).
 #pragma once
 
@@ -385,9 +385,6 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
 
 
 // ------------------------------------------------------------------ K2 ----
-template <typename T> struct Vec2;
-template <> struct Vec2<double> { typedef double2 type; };
-template <> struct Vec2<float> { typedef float2 type; };
 
 // Jacobi weight minus one of cell c (0 for interior cells)
 __device__ __forceinline__ int cell_class(const GeoL &G, unsigned int c) {
@@ -398,22 +395,68 @@ __device__ __forceinline__ int cell_class(const GeoL &G, unsigned int c) {
   return wall_count(i, G.nx, G.px) + 3 * wall_count(j, G.ny, G.py) + 9 * wall_count((int)k, G.nz, G.pz);
 }
 
-// One pair of cells: r -= alpha Ap; returns the new r.
-template <typename T, typename V2>
-__device__ __forceinline__ V2 update_pair(unsigned int q, T alpha, T *__restrict__ r, const T *__restrict__ Ap) {
-  const V2 av = reinterpret_cast<const V2 *>(Ap)[q];
-  V2 rv = reinterpret_cast<V2 *>(r)[q];
-  rv.x = fma(-alpha, av.x, rv.x);
-  rv.y = fma(-alpha, av.y, rv.y);
-  reinterpret_cast<V2 *>(r)[q] = rv;
-  return rv;
+// 16-byte vectors of the update kernel
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+  typedef float4 type;
+  static constexpr int E = 4;
+};
+template <> struct Vec16<double> {
+  typedef double2 type;
+  static constexpr int E = 2;
+};
+
+// r -= alpha Ap on one vector; the new r^2 go into acc (one FMA per cell)
+__device__ __forceinline__ void upd_vec(float4 &r, const float4 a, float alpha, float &acc) {
+  r.x = fmaf(-alpha, a.x, r.x);
+  r.y = fmaf(-alpha, a.y, r.y);
+  r.z = fmaf(-alpha, a.z, r.z);
+  r.w = fmaf(-alpha, a.w, r.w);
+  acc = fmaf(r.x, r.x, acc);
+  acc = fmaf(r.y, r.y, acc);
+  acc = fmaf(r.z, r.z, acc);
+  acc = fmaf(r.w, r.w, acc);
+}
+__device__ __forceinline__ void upd_vec(double2 &r, const double2 a, double alpha, double &acc) {
+  r.x = fma(-alpha, a.x, r.x);
+  r.y = fma(-alpha, a.y, r.y);
+  acc = fma(r.x, r.x, acc);
+  acc = fma(r.y, r.y, acc);
+}
+
+// r -= alpha Ap over the vectors [lo, hi) with the sum of r^2; two vectors
+// per thread per trip, both loaded before either is used
+template <typename T>
+__device__ __forceinline__ T upd_range(typename Vec16<T>::type *__restrict__ r4,
+                                       const typename Vec16<T>::type *__restrict__ a4, unsigned int lo,
+                                       unsigned int hi, unsigned int t0, unsigned int stride, T alpha) {
+  typedef typename Vec16<T>::type V;
+  T acc = 0;
+  for (unsigned int q = lo + t0; q < hi; q += 2 * stride) {
+    const unsigned int q2 = q + stride;
+    const bool two = q2 < hi;
+    V rv0 = r4[q];
+    const V av0 = a4[q];
+    V rv1, av1;
+    if (two) {
+      rv1 = r4[q2];
+      av1 = a4[q2];
+    }
+    upd_vec(rv0, av0, alpha, acc);
+    r4[q] = rv0;
+    if (two) {
+      upd_vec(rv1, av1, alpha, acc);
+      r4[q2] = rv1;
+    }
+  }
+  return acc;
 }
 
 // K2: r -= alpha Ap with (r,z) and (r,r); x += alpha p is left to the next
 // search kernel (or the settle / fold kernels), which reads p anyway.
 // (r,z) = (r,r) + sum over wall cells of (invL - 1) r^2.  Cells of interior
-// planes carry no class arithmetic: with periodic x and y the pairs of the two
-// z-wall planes run in loops of their own with one weight each.
+// planes carry no class arithmetic: with periodic x and y the vectors of the
+// two z-wall planes run in loops of their own with one weight each.
 template <typename T>
 __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r, const T *__restrict__ Ap,
                                                  DevState *st, double *partials, int cond) {
@@ -425,37 +468,27 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r
   load_tabs<T>(G, s_dL, s_inv);
   __syncthreads();
   typename Acc<T>::type rr = 0, corr = 0;
-  typedef typename Vec2<T>::type V2;
+  typedef typename Vec16<T>::type V;
+  constexpr int E = Vec16<T>::E;
   const unsigned int n = (unsigned int)G.n;
   const unsigned int stride = gridDim.x * FNT;
   const unsigned int t0 = blockIdx.x * FNT + threadIdx.x;
   const unsigned int plane = (unsigned int)G.nx * (unsigned int)G.ny;
-  if (G.px && G.py && !(n & 1) && !(plane & 1)) {
-    // pairs [lo, hi) of the interior planes, then the wall planes
-    const unsigned int wall_lo = G.pz ? 0u : plane / 2;                  // pairs in plane 0
-    const unsigned int wall_hi = G.pz ? n / 2 : (n - plane) / 2;         // first pair of plane nz-1
-    for (unsigned int q = wall_lo + t0; q < wall_hi; q += stride) {
-      const V2 rv = update_pair<T, V2>(q, alpha, r, Ap);
-      rr = fma(rv.x, rv.x, rr);
-      rr = fma(rv.y, rv.y, rr);
-    }
+  if (G.px && G.py && (plane % E) == 0) {
+    V *r4 = reinterpret_cast<V *>(r);
+    const V *a4 = reinterpret_cast<const V *>(Ap);
+    const unsigned int pv = plane / E, nv = n / E;
+    // vectors [wall_lo, wall_hi) of the interior planes, then the wall planes
+    const unsigned int wall_lo = G.pz ? 0u : pv;
+    const unsigned int wall_hi = G.pz ? nv : nv - pv;
+    rr = upd_range<T>(r4, a4, wall_lo, wall_hi, t0, stride, alpha);
     if (!G.pz) {
       const int wc = 9 * (G.nz == 1 ? 2 : 1);
       const T w = s_inv[wc] - T(1);
-      for (unsigned int q = t0; q < wall_lo; q += stride) {
-        const V2 rv = update_pair<T, V2>(q, alpha, r, Ap);
-        const T t = fma(rv.x, rv.x, rv.y * rv.y);
-        rr += t;
-        corr = fma(w, t, corr);
-      }
-      if (G.nz > 1) {
-        for (unsigned int q = wall_hi + t0; q < n / 2; q += stride) {
-          const V2 rv = update_pair<T, V2>(q, alpha, r, Ap);
-          const T t = fma(rv.x, rv.x, rv.y * rv.y);
-          rr += t;
-          corr = fma(w, t, corr);
-        }
-      }
+      T t = upd_range<T>(r4, a4, 0, wall_lo, t0, stride, alpha);
+      if (G.nz > 1) t += upd_range<T>(r4, a4, wall_hi, nv, t0, stride, alpha);
+      rr += t;
+      corr = w * t;
     }
   } else {
     // general walls: per-cell class

@@ -422,15 +422,19 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
   const int nx = G.nx, ny = G.ny, nz = G.nz;
   if (env_int("BBPP_TMA", 1) == 0) return;
   if (!encode_fn()) return;
+  // slab height: one float4 per thread per plane (NPT = 1) unless BBPP_TMA_NPT asks for 2 or 4
+  const int want = env_int("BBPP_TMA_NPT", 1);
   int ty;
-  if (nx <= 256 && nx % 32 == 0) ty = nx >= 256 ? 4 : 1024 / nx;
+  if (nx <= 256 && nx % 32 == 0) ty = (1024 / nx) * ((want == 2 || want == 4) ? want : 1);
   else if (nx % 256 == 0 && nx <= 1024) ty = 4;
   else return;
   if (ny % ty != 0 || ty > 256) return;
   const int npt = ty * nx / 1024;
   if (npt != 1 && npt != 2 && npt != 4) return;
   const int stage = 2 * (ty + 2) * nx * 4;
-  int ns = env_int("BBPP_TMA_NS", 6);
+  // 4 stages: one plane in flight beyond the three in use; more stages cost
+  // resident CTAs (measured at 256^3: 4 CTAs/SM with 4 stages beat deeper rings)
+  int ns = env_int("BBPP_TMA_NS", 4);
   ns = std::max(4, std::min(8, ns));  // >= 4: the refilled stage is never one of the three in use
   while (ns > 4 && ns * stage > kMaxStageBytes) ns--;
   if (ns * stage > kMaxStageBytes) return;
