@@ -32,6 +32,11 @@ WORKLOAD = ("C3: 256^3 cells, periodic x/y + Neumann z, 1000 spheres r=6 cells, 
 # the CUDA path and equal to the oracle's count; used to scale the bounded CPU
 # sample of the reference arm to a full solve.
 C3_FP64_ITERS = 604
+# DRAM bytes (read + write) per launch of the dominant kernels on this workload,
+# from one ncu capture each (profiles/k1_tma_k2_update_f32_c3_256.md,
+# profiles/k1_search2_k2_update_f64_c3_256.md): kernel kind -> bytes
+NCU_TRAFFIC = {"search_spmv_f32": 226.697984e6 + 150.230784e6, "search_spmv": 433.925632e6 + 353.379328e6,
+               "update_f32": 134.251008e6 + 20.922112e6, "update": 268.485376e6 + 92.526592e6}
 
 
 def peaks():
@@ -341,7 +346,8 @@ def run_ours(args):
         achieved = (kbytes / nl) / (kms / nl * 1e-3) / 1e9
         tot = sum(k[2] for k in ks)
         return {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hb, "unit": "GB/s",
-                "frac": achieved / hb, "traffic": None, "launches": nl, "avg_us": kms / nl * 1e3,
+                "frac": achieved / hb, "traffic": NCU_TRAFFIC.get(kname), "algorithmic_bytes": kbytes / nl,
+                "launches": nl, "avg_us": kms / nl * 1e3,
                 "share": kms / tot if tot else None,
                 "peak_source": "measured" if "fallback" not in pk else "fallback"}
 
