@@ -151,6 +151,35 @@ def train_c4_net(args):
     return net, info
 
 
+def reference_gpu(g, mask, rhs, tol, args):
+    """The reference's own CUDA solve (its kernels from oracle/_ref/ref_solver.cubin
+    under the restated one-rank host loop of src/cuda_solver.cu) on the same
+    workload and GPU, with its own stopping rule (r,z) <= tol^2 (b,b)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "refgpu"))
+    try:
+        import pyrefgpu
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": "harness import failed: %s" % e}
+    if not pyrefgpu.available():
+        return {"unavailable": "reference cubin not built (needs the reference tree at build time)"}
+    bc = tuple(int(v) for v in g.bc)
+    ref = pyrefgpu.RefSolver(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, bc, mask)
+    times, its = [], []
+    for i in range(2):
+        phi, it, res, ms, rc = ref.solve(rhs, tol)
+        if rc != 0:
+            ref.close()
+            return {"unavailable": "reference solve status %d" % rc}
+        times.append(ms)
+        its.append(it)
+    ref.close()
+    ms = float(np.mean(times[1:]))
+    return {"value": 1000.0 / ms, "unit": UNIT, "ms_per_solve": ms, "iters": its[-1],
+            "stop": "(r,z) <= tol^2 (b,b), the reference's rule",
+            "kind": "reference CUDA kernels (src/solver_kernel.cu, unmodified) on this GPU, one rank"}
+
+
 def profiler_api():
     """cuProfilerStart/Stop of the driver for the current context (a no-op
     where the driver library is missing)."""
@@ -362,6 +391,8 @@ def run_ours(args):
                "sample": "oracle PCG at 256^3 for 1 and 6 iterations (t_iter %.3f s); scaled to the %d "
                          "iterations plain FP64 PCG takes to 1e-8" % (info["t_iter_s"], plain["iters"])}
 
+    ref_gpu = reference_gpu(g, mask, rhs, tol, args) if rank == 0 and not args.no_cpu else None
+
     def canon_gbs(r):
         return r["bytes"] / (r["ms"] * 1e-3) / 1e9
 
@@ -392,6 +423,7 @@ def run_ours(args):
         "gpu_launches": H["launches"],
         "clocks": clk,
         "cpu_baseline": cpu,
+        "reference_gpu": ref_gpu,
     }
     if rank == 0:
         print(json.dumps(line))
