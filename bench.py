@@ -392,6 +392,14 @@ def run_ours(args):
                          "iterations plain FP64 PCG takes to 1e-8" % (info["t_iter_s"], plain["iters"])}
 
     ref_gpu = reference_gpu(g, mask, rhs, tol, args) if rank == 0 and not args.no_cpu else None
+    if ref_gpu is not None and "ms_per_solve" in ref_gpu:
+        # this library's plain FP64 PCG under the reference's stopping rule: the same work
+        reps = []
+        for _ in range(3):
+            reps.append(step(dict(precision=bbpp.FP64, stop=bbpp.STOP_REF_RZ)))
+        ref_gpu["ours_fp64_same_rule"] = {"ms_per_solve": float(np.mean([r.ms for r in reps[1:]])),
+                                          "iters": reps[-1].iters}
+        ref_gpu["speedup_fp64_same_rule"] = ref_gpu["ms_per_solve"] / ref_gpu["ours_fp64_same_rule"]["ms_per_solve"]
 
     def canon_gbs(r):
         return r["bytes"] / (r["ms"] * 1e-3) / 1e9

@@ -12,6 +12,15 @@
 
 namespace bbpp {
 
+// Programmatic dependent launch: wait until the preceding kernel of the stream
+// has finished and its writes are visible (a no-op without a programmatic
+// dependency), then let the next kernel start launching.  Every iteration
+// kernel calls it before it reads anything a predecessor wrote.
+__device__ __forceinline__ void pdl_sync() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Solve states written by the last CTA of a reduction kernel.
 enum DoneCode : int {
   RUNNING = 0,

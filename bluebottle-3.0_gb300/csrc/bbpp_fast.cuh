@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
   __shared__ T s_dL[27], s_inv[27];
   __shared__ __align__(16) T sp[3][PHY][PW];
   __shared__ double s_red[FNT / 32];
+  pdl_sync();
   if (*(volatile int *)&st->done) return;
   const bool first = *(volatile int *)&st->first;
   const T beta = first ? T(0) : (T)(*(volatile double *)&st->beta);
@@ -462,6 +463,7 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r
                                                  DevState *st, double *partials, int cond) {
   __shared__ T s_dL[27], s_inv[27];
   __shared__ double s_red[2 * FNT / 32];
+  pdl_sync();
   if (*(volatile int *)&st->done) return;
   if (cond && *(volatile int *)&st->rep_now) return;  // a checkpoint that replaces the residual
   const T alpha = (T)(*(volatile double *)&st->alpha);
@@ -518,6 +520,7 @@ __device__ __forceinline__ bool skip_step(const DevState *st, int check) {
 template <typename T>
 __global__ void __launch_bounds__(FNT) k_settle(const GeoL G, T *__restrict__ x, const T *__restrict__ p,
                                                 const DevState *st, int check) {
+  pdl_sync();
   if (skip_step(st, check)) return;
   if (!*(volatile const int *)&st->dlag) return;
   const T alpha = (T)(*(volatile const double *)&st->alpha);
@@ -537,6 +540,7 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
   __shared__ TXT sp[3][FHY][FHX];
   __shared__ uint8_t sm[3][FHY][FHX + 2];
   __shared__ double s_red[3 * FNT / 32];
+  pdl_sync();
   if (mode == 1 && skip_step(st, 2)) return;
   load_tabs<TXT>(G, s_dL, s_inv);
   const int tid = threadIdx.x;

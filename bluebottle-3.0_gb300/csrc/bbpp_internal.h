@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/bbpp.h"
@@ -83,7 +84,26 @@ struct bbpp_ctx {
   IrBuffers *ir = nullptr;
   NetWork *net = nullptr;
   bbpp_tma_state *tma = nullptr;  // launch shape and tensor maps of the TMA search kernel
+  bool pdl = false;               // iteration kernels launch with a programmatic dependency
 };
+
+// Launch an iteration kernel on ctx->stream; with ctx->pdl it may start while
+// its predecessor drains (the kernel's pdl_sync orders it after that kernel).
+template <typename... KArgs, typename... Args>
+inline void bbpp_launch(const bbpp_ctx *ctx, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                        Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = ctx->pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 void bbpp_record_error(bbpp_ctx *ctx, cudaError_t e, const char *what, int line);
 int bbpp_geo_init(const bbpp_grid *g, bbpp::Geo *G);

@@ -261,6 +261,13 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
   ctx->sms = dev_sms();
   stencil_shape(ctx);
   bbpp_tma_init(ctx);
+  {
+    // programmatic dependent launch of the iteration kernels: off unless
+    // BBPP_PDL=1 (measured at 256^3: no gain, the kernels' own drain and fill
+    // dominate the launch latency it hides)
+    const char *e = getenv("BBPP_PDL");
+    ctx->pdl = e && e[0] == '1';
+  }
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
       std::max<size_t>(std::max<size_t>((size_t)ctx->sgrid.x * ctx->sgrid.y * ctx->sgrid.z, (size_t)ctx->egrid),
@@ -389,16 +396,20 @@ static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, c
   } else {
     const dim3 g = ctx->pgrid[prec];
     const int kz = ctx->pkz[prec];
+    const dim3 b(FNT);
     if (mask) {
       if (ctx->GL.iso)
-        k1_search2<T, true, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+        bbpp_launch(ctx, k1_search2<T, true, true>, g, b, 0, ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
       else
-        k1_search2<T, true, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+        bbpp_launch(ctx, k1_search2<T, true, false>, g, b, 0, ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials,
+                    kz);
     } else {
       if (ctx->GL.iso)
-        k1_search2<T, false, true><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+        bbpp_launch(ctx, k1_search2<T, false, true>, g, b, 0, ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials,
+                    kz);
       else
-        k1_search2<T, false, false><<<g, FNT, 0, s>>>(ctx->GL, r, pold, pnew, Ap, x, mask, st, ctx->partials, kz);
+        bbpp_launch(ctx, k1_search2<T, false, false>, g, b, 0, ctx->GL, r, pold, pnew, Ap, x, mask, st,
+                    ctx->partials, kz);
     }
   }
   bbpp_rec_end(ctx);
@@ -409,7 +420,7 @@ template <typename T>
 static void launch_update(bbpp_ctx *ctx, T *r, const T *Ap, DevState *st, int cond) {
   // bytes/cell: read r, Ap, write r
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_UPDATE : KK_UPDATE_F32, 3.0 * sizeof(T));
-  k2_update<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, r, Ap, st, ctx->partials, cond);
+  bbpp_launch(ctx, k2_update<T>, dim3(ctx->egrid), dim3(FNT), 0, ctx->GL, r, Ap, st, ctx->partials, cond);
   bbpp_rec_end(ctx);
 }
 
@@ -430,22 +441,21 @@ void bbpp_launch_resid_s(bbpp_ctx *ctx, const uint8_t *mask, TXT *x, const TXT *
                          double bscale) {
   // bytes/cell: read x, rhs (+ mask), write r
   bbpp_rec_begin(ctx, sizeof(TXT) == 8 ? KK_RESID : KK_RESID_F32, 2.0 * sizeof(TXT) + sizeof(TR) + (mask ? 1 : 0));
-  const dim3 g = ctx->fgrid;
-  cudaStream_t s = ctx->stream;
+  const dim3 g = ctx->fgrid, b(FNT);
   if (mask) {
     if (ctx->GL.iso)
-      k_resid_s<TXT, TR, true, true><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz, mode,
-                                                       bscale);
+      bbpp_launch(ctx, k_resid_s<TXT, TR, true, true>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials,
+                  ctx->fkz, mode, bscale);
     else
-      k_resid_s<TXT, TR, true, false><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz, mode,
-                                                        bscale);
+      bbpp_launch(ctx, k_resid_s<TXT, TR, true, false>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials,
+                  ctx->fkz, mode, bscale);
   } else {
     if (ctx->GL.iso)
-      k_resid_s<TXT, TR, false, true><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz, mode,
-                                                        bscale);
+      bbpp_launch(ctx, k_resid_s<TXT, TR, false, true>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials,
+                  ctx->fkz, mode, bscale);
     else
-      k_resid_s<TXT, TR, false, false><<<g, FNT, 0, s>>>(ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz,
-                                                         mode, bscale);
+      bbpp_launch(ctx, k_resid_s<TXT, TR, false, false>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials,
+                  ctx->fkz, mode, bscale);
   }
   bbpp_rec_end(ctx);
 }
@@ -479,6 +489,7 @@ void bbpp_set_reliable(double *xhi, const double *rhs) {
 // lags), d = 0, all in FP64.  check as for k_settle.
 __global__ void __launch_bounds__(FNT) k_fold(const GeoL G, double *__restrict__ xhi, float *__restrict__ d,
                                               const float *__restrict__ p, const DevState *st, int check) {
+  pdl_sync();
   if (skip_step(st, check)) return;
   const bool lag = *(volatile const int *)&st->dlag;
   const double alpha = lag ? *(volatile const double *)&st->alpha : 0.0;
@@ -495,7 +506,7 @@ __global__ void __launch_bounds__(FNT) k_fold(const GeoL G, double *__restrict__
 template <typename T>
 static void launch_settle(bbpp_ctx *ctx, T *x, const T *p, DevState *st, int check) {
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_AXPY : KK_AXPY_F32, 3.0 * sizeof(T));
-  k_settle<T><<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, x, p, st, check);
+  bbpp_launch(ctx, k_settle<T>, dim3(ctx->egrid), dim3(FNT), 0, ctx->GL, x, p, st, check);
   bbpp_rec_end(ctx);
 }
 
@@ -507,7 +518,8 @@ static void launch_replace(bbpp_ctx *ctx, const uint8_t *mask, T *x, const T *rh
   const int check = mode == RES_ITER ? 2 : 0;
   if (sizeof(T) == 4 && t_rel.xhi) {
     bbpp_rec_begin(ctx, KK_AXPY_F32, 20.0);
-    k_fold<<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, t_rel.xhi, (float *)x, (const float *)p, st, check);
+    bbpp_launch(ctx, k_fold, dim3(ctx->egrid), dim3(FNT), 0, ctx->GL, t_rel.xhi, (float *)x, (const float *)p, st,
+                check);
     bbpp_rec_end(ctx);
     bbpp_launch_resid_s<double, float>(ctx, mask, t_rel.xhi, t_rel.rhs, (float *)r, st, mode, ctx->GL.S);
   } else {

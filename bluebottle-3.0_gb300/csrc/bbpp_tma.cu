@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   __shared__ float s_dL[27], s_inv[27];
   __shared__ double s_red[TNT / 32];
   __shared__ unsigned long long s_full[8];
+  pdl_sync();
   if (*(volatile int *)&st->done) return;
   const bool first = *(volatile int *)&st->first;
   const float beta = first ? 0.f : (float)(*(volatile double *)&st->beta);
@@ -518,10 +519,9 @@ bool bbpp_tma_search(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const f
   M.r_row = mr.row;
   M.p_rows = mp.rows;
   M.p_row = mp.row;
-  cudaStream_t s = ctx->stream;
-#define BBPP_TMA_LAUNCH(N, MK, IS)                                                                        \
-  k1_tma<N, MK, IS><<<t->grid, TNT, t->smem, s>>>(ctx->GL, M, pnew, Ap, x, mask, st, ctx->partials, t->ty, \
-                                                  t->kz, t->ns, t->four_d)
+#define BBPP_TMA_LAUNCH(N, MK, IS)                                                                          \
+  bbpp_launch(ctx, k1_tma<N, MK, IS>, t->grid, dim3(TNT), (size_t)t->smem, ctx->GL, M, pnew, Ap, x, mask, st, \
+              ctx->partials, t->ty, t->kz, t->ns, t->four_d)
 #define BBPP_TMA_NPT(N)                            \
   if (mask) {                                      \
     if (ctx->GL.iso) BBPP_TMA_LAUNCH(N, true, true);   \
