@@ -128,6 +128,7 @@ def lib():
         "bbpp_rng_uniform": (None, [ctypes.c_ulonglong, ctypes.c_longlong, D, D, P]),
         "bbpp_rng_gauss": (None, [ctypes.c_ulonglong, ctypes.c_longlong, P]),
         "bbpp_version": (ctypes.c_char_p, []),
+        "bbpp_set_device": (I, [I]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

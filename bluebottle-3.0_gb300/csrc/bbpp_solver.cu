@@ -381,6 +381,15 @@ extern "C" const char *bbpp_last_error(const bbpp_ctx *ctx) {
 
 extern "C" const char *bbpp_version(void) { return "bbpp 0.1 (sm_103a)"; }
 
+// The GPU this host thread's later contexts and buffers use (one process per
+// GPU: the process's local rank).
+extern "C" int bbpp_set_device(int device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return BBPP_NO_DEVICE;
+  if (device < 0 || device >= n) return BBPP_BAD_ARG;
+  return cudaSetDevice(device) == cudaSuccess ? 0 : BBPP_CUDA_ERROR;
+}
+
 // ---------------------------------------------------------------- launches --
 // All launches go to ctx->stream.  Typed on the vector element.
 template <typename T>

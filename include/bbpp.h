@@ -240,6 +240,9 @@ void bbpp_rng_gauss(unsigned long long seed, long long n, double *out);
 
 /* Library version string. */
 const char *bbpp_version(void);
+/* Select the GPU for this host thread's later contexts and buffers (one process per GPU; no counterpart in
+ * the reference, whose ranks each own one GPU through cudaSetDevice in its start-up code). */
+int bbpp_set_device(int device);
 
 #ifdef __cplusplus
 }
