@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <sys/time.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -291,7 +292,196 @@ void solve(bool particles, bool timed) {
   record(rep.iters, sqrt(rep.rz) / sqrt(rep.bb), etime);
 }
 
+// ------------------------------------------------------------ epilogue --
+// The time loop's steps after the solve (src/bluebottle.c:233-252): ghosts of
+// phi, the projection of u*, and the pressure update.  The arithmetic is the
+// reference kernels' (src/bluebottle_kernel.cu) in their evaluation order with
+// no contraction, so u, v, w and the ghosts equal the reference's bit for bit;
+// the pressure mean is a deterministic block-ordered sum.
+
+// cuda_dom_BC_p: on a Neumann face the ghost is the adjacent interior cell
+// (BC_p_W_N .. BC_p_T_N, src/bluebottle_kernel.cu:26-102).  blockIdx.y = face.
+__global__ void k_dom_bc_p(Shape S, int faces, double *__restrict__ a) {
+  const int f = blockIdx.y;
+  if (!((faces >> f) & 1)) return;
+  const int nx = S.nx, ny = S.ny, nz = S.nz;
+  const long long n = f < 2 ? (long long)ny * nz : (f < 4 ? (long long)nx * nz : (long long)nx * ny);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    long long dst, src;
+    if (f < 2) {  // W, E: (j, k)
+      const int j = 1 + (int)(t % ny), k = 1 + (int)(t / ny);
+      const long long row = (long long)j * S.s1b + (long long)k * S.s2b;
+      dst = row + (f == 0 ? 0 : nx + 1);
+      src = row + (f == 0 ? 1 : nx);
+    } else if (f < 4) {  // S, N: (i, k)
+      const int i = 1 + (int)(t % nx), k = 1 + (int)(t / nx);
+      const long long col = i + (long long)k * S.s2b;
+      dst = col + (long long)(f == 2 ? 0 : ny + 1) * S.s1b;
+      src = col + (long long)(f == 2 ? 1 : ny) * S.s1b;
+    } else {  // B, T: (i, j)
+      const int i = 1 + (int)(t % nx), j = 1 + (int)(t / nx);
+      const long long col = i + (long long)j * S.s1b;
+      dst = col + (long long)(f == 4 ? 0 : nz + 1) * S.s2b;
+      src = col + (long long)(f == 4 ? 1 : nz) * S.s2b;
+    }
+    a[dst] = a[src];
+  }
+}
+
+// u = u* - (dt/rho) |flag| ddx (phi_c - phi_w) on every x face
+// (project_u, src/bluebottle_kernel.cu:2303-2319); threads follow the face
+// array's own order (GFX_LOC = j + k s1b + i s2b: j fastest).
+__global__ void k_project_x(Shape S, double dtr, double dd, const double *__restrict__ us,
+                            const double *__restrict__ phi, const int *__restrict__ flag, double *__restrict__ u) {
+  const int nx = S.nx, ny = S.ny, nz = S.nz;
+  const long long n = (long long)(nx + 1) * ny * nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int j = 1 + (int)(t % ny);
+    const long long r = t / ny;
+    const int k = 1 + (int)(r % nz), i = 1 + (int)(r / nz);
+    const long long f = j + (long long)k * S.fx_s1b + (long long)i * S.fx_s2b;
+    const long long cc = i + (long long)j * S.s1b + (long long)k * S.s2b;
+    const double grad = __dmul_rn(__dmul_rn((double)abs(flag[f]), dd), __dsub_rn(phi[cc], phi[cc - 1]));
+    u[f] = __dsub_rn(us[f], __dmul_rn(dtr, grad));
+  }
+}
+
+// v faces (project_v): GFY_LOC = k + i s1b + j s2b, k fastest
+__global__ void k_project_y(Shape S, double dtr, double dd, const double *__restrict__ vs,
+                            const double *__restrict__ phi, const int *__restrict__ flag, double *__restrict__ v) {
+  const int nx = S.nx, ny = S.ny, nz = S.nz;
+  const long long n = (long long)nx * (ny + 1) * nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int k = 1 + (int)(t % nz);
+    const long long r = t / nz;
+    const int i = 1 + (int)(r % nx), j = 1 + (int)(r / nx);
+    const long long f = k + (long long)i * S.fy_s1b + (long long)j * S.fy_s2b;
+    const long long cc = i + (long long)j * S.s1b + (long long)k * S.s2b;
+    const double grad = __dmul_rn(__dmul_rn((double)abs(flag[f]), dd), __dsub_rn(phi[cc], phi[cc - S.s1b]));
+    v[f] = __dsub_rn(vs[f], __dmul_rn(dtr, grad));
+  }
+}
+
+// w faces (project_w): GFZ_LOC = i + j s1b + k s2b, i fastest
+__global__ void k_project_z(Shape S, double dtr, double dd, const double *__restrict__ ws,
+                            const double *__restrict__ phi, const int *__restrict__ flag, double *__restrict__ w) {
+  const int nx = S.nx, ny = S.ny, nz = S.nz;
+  const long long n = (long long)nx * ny * (nz + 1);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % nx);
+    const long long r = t / nx;
+    const int j = 1 + (int)(r % ny), k = 1 + (int)(r / ny);
+    const long long f = i + (long long)j * S.fz_s1b + (long long)k * S.fz_s2b;
+    const long long cc = i + (long long)j * S.s1b + (long long)k * S.s2b;
+    const double grad = __dmul_rn(__dmul_rn((double)abs(flag[f]), dd), __dsub_rn(phi[cc], phi[cc - S.s2b]));
+    w[f] = __dsub_rn(ws[f], __dmul_rn(dtr, grad));
+  }
+}
+
+// p = (fluid) (p0 + phi) on the interior (update_p, src/bluebottle_kernel.cu:
+// 2385-2402) with the block partial sums of p; the last block to finish
+// leaves -mean in *neg_mean.
+__global__ void __launch_bounds__(256) k_update_p(Shape S, const double *__restrict__ p0,
+                                                  const double *__restrict__ phi, const int *__restrict__ phase,
+                                                  double *__restrict__ p, double *partials, unsigned int *ticket,
+                                                  double *neg_mean) {
+  __shared__ double s_sum[8];
+  __shared__ int s_last;
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  double acc = 0.0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % S.nx);
+    const long long r = c / S.nx;
+    const int j = (int)(r % S.ny), k = (int)(r / S.ny);
+    const long long C = gcc_b(i, j, k, S.s1b, S.s2b);
+    const double v = __dmul_rn((double)(phase[C] < 0), __dadd_rn(p0[C], phi[C]));
+    p[C] = v;
+    acc += v;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_sum[w];
+    partials[blockIdx.x] = t;
+    __threadfence();
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    double t = 0.0;
+    for (unsigned int b = 0; b < gridDim.x; b++) t += __ldcg(&partials[b]);
+    *neg_mean = -(t / (double)n);
+    *ticket = 0;
+  }
+}
+
+// p += -mean on the interior (forcing_add_c_const, src/bluebottle_kernel.cu:1507)
+__global__ void k_add_const(Shape S, const double *__restrict__ neg_mean, double *__restrict__ p) {
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  const double v = *neg_mean;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % S.nx);
+    const long long r = c / S.nx;
+    const int j = (int)(r % S.ny), k = (int)(r / S.ny);
+    const long long C = gcc_b(i, j, k, S.s1b, S.s2b);
+    p[C] = __dadd_rn(p[C], v);
+  }
+}
+
+struct Epi {
+  double *partials = nullptr;  // one per block of k_update_p, then -mean
+  unsigned int *ticket = nullptr;
+};
+Epi e_ws;
+constexpr int kEpiBlocks = 1024;
+
 }  // namespace
+
+extern "C" void cuda_dom_BC_p(bb_real *array) {
+  if (nprocs != 1) {
+    fprintf(stderr, "N%d >> bbpp: one rank per GPU only (nprocs = %d)\n", rank, nprocs);
+    exit(EXIT_FAILURE);
+  }
+  const Shape S = shape_of(dom[rank]);
+  // one rank: a face is a domain boundary exactly when its direction is not periodic
+  const int faces = (bc.pW == BBPP_NEUMANN) | (bc.pE == BBPP_NEUMANN) << 1 | (bc.pS == BBPP_NEUMANN) << 2 |
+                    (bc.pN == BBPP_NEUMANN) << 3 | (bc.pB == BBPP_NEUMANN) << 4 | (bc.pT == BBPP_NEUMANN) << 5;
+  if (!faces) return;
+  const long long mx = std::max<long long>(std::max<long long>((long long)S.ny * S.nz, (long long)S.nx * S.nz),
+                                           (long long)S.nx * S.ny);
+  k_dom_bc_p<<<dim3(grid_blocks(mx), 6), 256>>>(S, faces, array);
+  check(cudaGetLastError(), "dom_BC_p kernel");
+}
+
+extern "C" void cuda_project(void) {
+  const bb_dom_struct &d = dom[rank];
+  const Shape S = shape_of(d);
+  const double dtr = dt / rho_f;
+  k_project_x<<<grid_blocks((long long)(S.nx + 1) * S.ny * S.nz), 256>>>(S, dtr, 1. / d.dx, _u_star, _phi, _flag_u,
+                                                                           _u);
+  k_project_y<<<grid_blocks((long long)S.nx * (S.ny + 1) * S.nz), 256>>>(S, dtr, 1. / d.dy, _v_star, _phi, _flag_v,
+                                                                           _v);
+  k_project_z<<<grid_blocks((long long)S.nx * S.ny * (S.nz + 1)), 256>>>(S, dtr, 1. / d.dz, _w_star, _phi, _flag_w,
+                                                                           _w);
+  check(cudaGetLastError(), "project kernels");
+}
+
+extern "C" void cuda_update_p(void) {
+  const Shape S = shape_of(dom[rank]);
+  if (!e_ws.partials) {
+    check(cudaMalloc(&e_ws.partials, sizeof(double) * (kEpiBlocks + 1)), "epilogue workspace");
+    check(cudaMalloc(&e_ws.ticket, sizeof(unsigned int)), "epilogue workspace");
+    check(cudaMemset(e_ws.ticket, 0, sizeof(unsigned int)), "epilogue workspace");
+  }
+  const long long n = (long long)S.nx * S.ny * S.nz;
+  const int nb = std::min(kEpiBlocks, grid_blocks(n));
+  k_update_p<<<nb, 256>>>(S, _p0, _phi, _phase, _p, e_ws.partials, e_ws.ticket, e_ws.partials + kEpiBlocks);
+  k_add_const<<<grid_blocks(n), 256>>>(S, e_ws.partials + kEpiBlocks, _p);
+  check(cudaGetLastError(), "update_p kernels");
+}
 
 extern "C" void bbpp_bluebottle_release(void) {
   if (g.ctx) bbpp_destroy(g.ctx);
@@ -299,6 +489,9 @@ extern "C" void bbpp_bluebottle_release(void) {
   if (g.b) cudaFree(g.b);
   if (g.x) cudaFree(g.x);
   g = DropIn();
+  if (e_ws.partials) cudaFree(e_ws.partials);
+  if (e_ws.ticket) cudaFree(e_ws.ticket);
+  e_ws = Epi();
 }
 
 extern "C" void cuda_PP_init_jacobi_preconditioner(void) {

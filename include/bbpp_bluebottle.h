@@ -83,6 +83,17 @@ void cuda_PP_cg_noparts(void);
  * kernel (plus residual replacements), and ip1/ar1/ip2/ar2/up2/mpi are 0. */
 void cuda_PP_cg_timed(void);
 
+/* The time loop's steps after the solve (src/bluebottle.c:233-252), same names and
+ * signatures as src/cuda_bluebottle.cu:2495-2589, one rank:
+ *  cuda_dom_BC_p(array): Neumann ghost planes of a cell array = the adjacent interior
+ *    cells (periodic ghosts are the host's mpi_cuda_exchange_Gcc);
+ *  cuda_project(): u, v, w = u*, v*, w* - dt/rho_f |flag| grad(_phi) on every face;
+ *  cuda_update_p(): _p = (fluid) (_p0 + _phi) on the interior, minus its mean over all cells.
+ * All launch on the default stream, as the reference's. */
+void cuda_dom_BC_p(bb_real *array);
+void cuda_project(void);
+void cuda_update_p(void);
+
 /* Free the library's private device workspace (no counterpart in the
  * reference, whose solver uses the host program's buffers). */
 void bbpp_bluebottle_release(void);
@@ -102,6 +113,8 @@ extern int stepnum;
 extern bb_real *_phi, *_rhs_p, *_invM;
 extern bb_real *_u_star, *_v_star, *_w_star;
 extern int *_phase;
+extern bb_real *_u, *_v, *_w, *_p, *_p0;  /* the epilogue's fields */
+extern int *_flag_u, *_flag_v, *_flag_w;
 /* ---- functions of the host program the solver calls ---- */
 void cuda_part_BC_p(void);                                              /* src/cuda_particle.cu:1679 */
 void recorder_PP(char *name, int niter, bb_real resid, bb_real etime);  /* src/recorder.c:190 */

@@ -427,3 +427,58 @@ void orc_rhs_mask_refine(const orc_grid *g, const uint8_t *solid, double *rhs)
   memcpy(rhs, out, sizeof(double) * (size_t)n);
   free(out);
 }
+
+/* ------------------------------------------------------------ epilogue --- */
+/* phi at cell index g (may be -1 or n: a ghost): periodic wrap, or the
+ * adjacent interior cell (Neumann ghost, BC_p_*_N) */
+static inline int ghost_cell(int g, int n, int periodic)
+{
+  if (g < 0) return periodic ? n - 1 : 0;
+  if (g >= n) return periodic ? 0 : n - 1;
+  return g;
+}
+
+void orc_epilogue(const orc_grid *g, const uint8_t *solid, double rho_f, double dt, const double *phi,
+                  const double *us, const double *vs, const double *ws, const double *p0, double *u, double *v,
+                  double *w, double *p)
+{
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const int px = g->bc[0] == 0, py = g->bc[2] == 0, pz = g->bc[4] == 0;
+  const double ddx = 1. / g->dx, ddy = 1. / g->dy, ddz = 1. / g->dz;
+#define PHI(i, j, k) phi[(long long)(i) + (long long)nx * ((j) + (long long)ny * (k))]
+  /* project_u: faces i = 0..nx between cells i-1 and i */
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i <= nx; i++) {
+        const int fl = px || (i > 0 && i < nx); /* |flag_u| */
+        const double grad = (double)fl * ddx * (PHI(ghost_cell(i, nx, px), j, k) - PHI(ghost_cell(i - 1, nx, px), j, k));
+        const long long f = i + (long long)(nx + 1) * (j + (long long)ny * k);
+        u[f] = us[f] - dt / rho_f * grad;
+      }
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j <= ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const int fl = py || (j > 0 && j < ny);
+        const double grad = (double)fl * ddy * (PHI(i, ghost_cell(j, ny, py), k) - PHI(i, ghost_cell(j - 1, ny, py), k));
+        const long long f = i + (long long)nx * (j + (long long)(ny + 1) * k);
+        v[f] = vs[f] - dt / rho_f * grad;
+      }
+  for (int k = 0; k <= nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const int fl = pz || (k > 0 && k < nz);
+        const double grad = (double)fl * ddz * (PHI(i, j, ghost_cell(k, nz, pz)) - PHI(i, j, ghost_cell(k - 1, nz, pz)));
+        const long long f = i + (long long)nx * (j + (long long)ny * k);
+        w[f] = ws[f] - dt / rho_f * grad;
+      }
+#undef PHI
+  /* update_p and the mean removal: a sequential sum in cell order */
+  const long long n = (long long)nx * ny * nz;
+  double s = 0.;
+  for (long long c = 0; c < n; c++) {
+    p[c] = (double)(!solid || !solid[c]) * (p0[c] + phi[c]);
+    s += p[c];
+  }
+  const double mean = s / (double)n;
+  for (long long c = 0; c < n; c++) p[c] += -mean;
+}

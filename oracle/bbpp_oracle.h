@@ -94,6 +94,20 @@ void orc_rhs_div(const orc_grid *g, double rho_f, double dt, const double *u,
  * coeffs_refine (src/solver_kernel.cu:212-256). */
 void orc_rhs_mask_refine(const orc_grid *g, const uint8_t *solid, double *rhs);
 
+/* The time loop's steps after the solve on one rank (src/bluebottle.c:233-252):
+ * phi's ghosts (periodic: opposite interior plane, mpi_cuda_exchange_Gcc;
+ * Neumann: adjacent interior cell, BC_p_*_N, src/bluebottle_kernel.cu:26-102),
+ * the projection u = u* - dt/rho |flag| dphi/dx on every face
+ * (project_u/v/w, src/bluebottle_kernel.cu:2303-2355; |flag| = 0 only on a wall
+ * face of a non-periodic direction), and the pressure update
+ * p = (fluid) (p0 + phi) minus its mean over all cells (update_p,
+ * copy_p_p_noghost, forcing_add_c_const, src/cuda_bluebottle.cu:2506-2536).
+ * Dense arrays: cells as above; faces u[i + (nx+1)(j + ny k)], i = 0..nx,
+ * v[i + nx(j + (ny+1) k)], w[i + nx(j + ny k)], k = 0..nz (as orc_rhs_div). */
+void orc_epilogue(const orc_grid *g, const uint8_t *solid, double rho_f, double dt, const double *phi,
+                  const double *us, const double *vs, const double *ws, const double *p0, double *u, double *v,
+                  double *w, double *p);
+
 #ifdef __cplusplus
 }
 #endif

@@ -56,6 +56,8 @@ def lib():
                                       ctypes.c_int, P, P, P, P, P]
         L.orc_rhs_div.argtypes = [ctypes.POINTER(OrcGrid), ctypes.c_double, ctypes.c_double, P, P, P, P]
         L.orc_rhs_mask_refine.argtypes = [ctypes.POINTER(OrcGrid), P, P]
+        L.orc_epilogue.argtypes = [ctypes.POINTER(OrcGrid), P, ctypes.c_double, ctypes.c_double, P, P, P, P, P, P, P,
+                                   P, P]
         L.orc_grid_check.argtypes = [ctypes.POINTER(OrcGrid)]
         L.orc_grid_check.restype = ctypes.c_int
         _L = L
@@ -147,3 +149,17 @@ def rhs_mask_refine(g, mask, rhs):
     out = _c(rhs, np.float64).copy()
     lib().orc_rhs_mask_refine(ctypes.byref(g), _p(_c(mask, np.uint8)), _p(out))
     return out
+
+
+def epilogue(g, mask, rho_f, dt, phi, us, vs, ws, p0):
+    """Post-solve steps (ghosts of phi, projection, pressure update): dense
+    cells and faces as orc_rhs_div; returns (u, v, w, p)."""
+    u = np.empty_like(_c(us, np.float64))
+    v = np.empty_like(_c(vs, np.float64))
+    w = np.empty_like(_c(ws, np.float64))
+    p = np.empty_like(_c(p0, np.float64))
+    m = None if mask is None else _c(mask, np.uint8)
+    lib().orc_epilogue(ctypes.byref(g), _p(m), ctypes.c_double(rho_f), ctypes.c_double(dt), _p(_c(phi, np.float64)),
+                       _p(_c(us, np.float64)), _p(_c(vs, np.float64)), _p(_c(ws, np.float64)),
+                       _p(_c(p0, np.float64)), _p(u), _p(v), _p(w), _p(p))
+    return u, v, w, p

@@ -1,6 +1,7 @@
 """Host build of the reference pressure solver, used to pin the oracle.
 
-Compiles the unmodified src/cuda_solver.cu and src/solver_kernel.cu from the
+Compiles the unmodified src/cuda_solver.cu, src/solver_kernel.cu and
+src/bluebottle_kernel.cu (the post-solve epilogue's kernels) from the
 reference tree for the CPU, with the shims in oracle/ref/shim (CUDA execution
 model as fibers, one-rank MPI, thrust::inner_product) and the harness in
 oracle/ref/harness.cpp, into oracle/_ref/libref.so.  Kernel launches
@@ -81,9 +82,11 @@ def build():
         print("reference tree not found (%s); oracle/_ref not built" % SRC)
         return None
     os.makedirs(OUT, exist_ok=True)
-    objs = [os.path.join(OUT, n) for n in ("cuda_solver.o", "solver_kernel.o", "harness.o", "emu_runtime.o")]
+    objs = [os.path.join(OUT, n) for n in ("cuda_solver.o", "solver_kernel.o", "harness.o", "emu_runtime.o",
+                                           "bluebottle_kernel.o")]
     compile_ref("cuda_solver.cu", objs[0], ["-DPP_rhs=PP_rhs_inject"])
     compile_ref("solver_kernel.cu", objs[1])
+    compile_ref("bluebottle_kernel.cu", objs[4])
     compile_own("harness.cpp", objs[2])
     compile_own("emu_runtime.cpp", objs[3])
     lib = os.path.join(OUT, "libref.so")

@@ -16,11 +16,13 @@ extern "C" {
 #include "recorder.h"
 }
 #include "cuda_solver.h"
+#include "cuda_bluebottle.h"
 
 // ------------------------------------------------------------- globals ----
 dom_struct DOM;
 dom_struct *dom = nullptr;
 dom_struct _dom;
+bin_struct _bins;  // read by particle kernels of src/bluebottle_kernel.cu, never by the ones used here
 cuda_blocks_struct blocks;
 BC bc;
 int rank = 0;
@@ -32,6 +34,7 @@ int stepnum = 0;
 real pp_residual = 1e-8;
 int pp_max_iter = 20000;
 real *_phi, *_rhs_p, *_r_q, *_z_q, *_p_q, *_pb_q, *_Apb_q, *_invM, *_u_star, *_v_star, *_w_star;
+real *_u, *_v, *_w, *_p, *_p0;  // the post-solve epilogue's fields
 int *_flag_u, *_flag_v, *_flag_w, *_phase, *_phase_shell;
 
 static std::vector<double> g_inject;  // dense rhs to inject (nz, ny, nx)
@@ -131,9 +134,11 @@ static int cdiv(int a, int b) { return (a + b - 1) / b; }
 static void release() {
   for (void *p : {(void *)_phi, (void *)_rhs_p, (void *)_r_q, (void *)_z_q, (void *)_p_q, (void *)_pb_q,
                   (void *)_Apb_q, (void *)_invM, (void *)_u_star, (void *)_v_star, (void *)_w_star,
-                  (void *)_flag_u, (void *)_flag_v, (void *)_flag_w, (void *)_phase, (void *)_phase_shell})
+                  (void *)_flag_u, (void *)_flag_v, (void *)_flag_w, (void *)_phase, (void *)_phase_shell,
+                  (void *)_u, (void *)_v, (void *)_w, (void *)_p, (void *)_p0})
     free(p);
   _phi = _rhs_p = _r_q = _z_q = _p_q = _pb_q = _Apb_q = _invM = _u_star = _v_star = _w_star = nullptr;
+  _u = _v = _w = _p = _p0 = nullptr;
   _flag_u = _flag_v = _flag_w = _phase = _phase_shell = nullptr;
   delete[] dom;
   dom = nullptr;
@@ -181,6 +186,18 @@ extern "C" int ref_setup(int nx, int ny, int nz, double dx, double dy, double dz
   blocks.Gcc.dim_inb = dim3(ty, tz); blocks.Gcc.num_inb = dim3(cdiv(G.jnb, ty), cdiv(G.knb, tz));
   blocks.Gcc.dim_jnb = dim3(tz, tx); blocks.Gcc.num_jnb = dim3(cdiv(G.knb, tz), cdiv(G.inb, tx));
   blocks.Gcc.dim_knb = dim3(tx, ty); blocks.Gcc.num_knb = dim3(cdiv(G.inb, tx), cdiv(G.jnb, ty));
+  // in / jn / kn shapes of every grid (cuda_blocks_init, src/cuda_bluebottle.cu:511-790)
+  auto faces = [](const grid_info &F, cuda_blocks_info &B) {
+    const int fx = threads_of(F.in), fy = threads_of(F.jn), fz = threads_of(F.kn);
+    const int bx = cdiv(F.in, fx), by = cdiv(F.jn, fy), bz = cdiv(F.kn, fz);
+    B.dim_in = dim3(fy, fz); B.num_in = dim3(by, bz);
+    B.dim_jn = dim3(fz, fx); B.num_jn = dim3(bz, bx);
+    B.dim_kn = dim3(fx, fy); B.num_kn = dim3(bx, by);
+  };
+  faces(d.Gcc, blocks.Gcc);
+  faces(d.Gfx, blocks.Gfx);
+  faces(d.Gfy, blocks.Gfy);
+  faces(d.Gfz, blocks.Gfz);
 
   _phi = (real *)calloc(G.s3b, sizeof(real));
   _rhs_p = (real *)calloc(G.s3b, sizeof(real));
@@ -193,6 +210,11 @@ extern "C" int ref_setup(int nx, int ny, int nz, double dx, double dy, double dz
   _u_star = (real *)calloc(d.Gfx.s3b, sizeof(real));
   _v_star = (real *)calloc(d.Gfy.s3b, sizeof(real));
   _w_star = (real *)calloc(d.Gfz.s3b, sizeof(real));
+  _u = (real *)calloc(d.Gfx.s3b, sizeof(real));
+  _v = (real *)calloc(d.Gfy.s3b, sizeof(real));
+  _w = (real *)calloc(d.Gfz.s3b, sizeof(real));
+  _p = (real *)calloc(G.s3b, sizeof(real));
+  _p0 = (real *)calloc(G.s3b, sizeof(real));
   _phase = (int *)malloc(sizeof(int) * G.s3b);
   _phase_shell = (int *)malloc(sizeof(int) * G.s3b);
   _flag_u = (int *)malloc(sizeof(int) * d.Gfx.s3b);
@@ -354,4 +376,82 @@ extern "C" int ref_rhs(double rho, double dtt, const double *u, const double *v,
     for (int j = 0; j < ny; j++)
       for (int i = 0; i < nx; i++) rhs[(size_t)i + (size_t)nx * (j + (size_t)ny * k)] = _rhs_p[ccb(i, j, k)];
   return 0;
+}
+
+// ------------------------------------------------------------- epilogue --
+// The time loop's steps after the solve (src/bluebottle.c:233-252, one rank):
+// mpi_cuda_exchange_Gcc(_phi); cuda_dom_BC_p(_phi); cuda_project(); and
+// cuda_update_p() (src/cuda_bluebottle.cu:2495-2589), with the reference's
+// kernels BC_p_*_N, project_u/v/w, update_p_laplacian, update_p,
+// copy_p_p_noghost and forcing_add_c_const (src/bluebottle_kernel.cu).
+// The host sequencing of those three functions is restated here; thrust's
+// reduce of the pressure mean is a plain sum.  Inputs: phi (dense interior),
+// u*, v*, w* and p0 as ghosted s3b arrays of their grids; outputs: the
+// ghost-filled phi (s3b), u, v, w (face s3b) and p (s3b).
+extern "C" int ref_epilogue(double rho, double dtt, double nu_, const double *phi, const double *us,
+                            const double *vs, const double *ws, const double *p0, double *phi_b, double *u, double *v,
+                            double *w, double *p) {
+  const dom_struct &d = dom[0];
+  const grid_info &G = d.Gcc;
+  rho_f = rho;
+  dt = dtt;
+  nu = nu_;
+  memset(_phi, 0, sizeof(real) * G.s3b);
+  for (int k = 0; k < G.kn; k++)
+    for (int j = 0; j < G.jn; j++)
+      for (int i = 0; i < G.in; i++) _phi[ccb(i, j, k)] = phi[(size_t)i + (size_t)G.in * (j + (size_t)G.jn * k)];
+  memcpy(_u_star, us, sizeof(real) * d.Gfx.s3b);
+  memcpy(_v_star, vs, sizeof(real) * d.Gfy.s3b);
+  memcpy(_w_star, ws, sizeof(real) * d.Gfz.s3b);
+  memcpy(_p0, p0, sizeof(real) * G.s3b);
+  memset(_u, 0, sizeof(real) * d.Gfx.s3b);
+  memset(_v, 0, sizeof(real) * d.Gfy.s3b);
+  memset(_w, 0, sizeof(real) * d.Gfz.s3b);
+  memset(_p, 0, sizeof(real) * G.s3b);
+  // mpi_cuda_exchange_Gcc(_phi); cuda_dom_BC_p(_phi): Neumann faces of one rank
+  mpi_cuda_exchange_Gcc(_phi);
+  if (bc.pW == NEUMANN) emu::launch(blocks.Gcc.num_in, blocks.Gcc.dim_in, [&] { BC_p_W_N(_phi); });
+  if (bc.pE == NEUMANN) emu::launch(blocks.Gcc.num_in, blocks.Gcc.dim_in, [&] { BC_p_E_N(_phi); });
+  if (bc.pS == NEUMANN) emu::launch(blocks.Gcc.num_jn, blocks.Gcc.dim_jn, [&] { BC_p_S_N(_phi); });
+  if (bc.pN == NEUMANN) emu::launch(blocks.Gcc.num_jn, blocks.Gcc.dim_jn, [&] { BC_p_N_N(_phi); });
+  if (bc.pB == NEUMANN) emu::launch(blocks.Gcc.num_kn, blocks.Gcc.dim_kn, [&] { BC_p_B_N(_phi); });
+  if (bc.pT == NEUMANN) emu::launch(blocks.Gcc.num_kn, blocks.Gcc.dim_kn, [&] { BC_p_T_N(_phi); });
+  // cuda_project
+  emu::launch(blocks.Gfx.num_in, blocks.Gfx.dim_in,
+              [&] { project_u(_u_star, _phi, rho_f, dt, _u, 1. / d.dx, _flag_u); });
+  emu::launch(blocks.Gfy.num_jn, blocks.Gfy.dim_jn,
+              [&] { project_v(_v_star, _phi, rho_f, dt, _v, 1. / d.dy, _flag_v); });
+  emu::launch(blocks.Gfz.num_kn, blocks.Gfz.dim_kn,
+              [&] { project_w(_w_star, _phi, rho_f, dt, _w, 1. / d.dz, _flag_w); });
+  // cuda_update_p
+  std::vector<real> Lp((size_t)G.s3b, 0.), pm((size_t)G.s3, 0.);
+  emu::launch(blocks.Gcc.num_kn, blocks.Gcc.dim_kn, [&] { update_p_laplacian(Lp.data(), _phi); });
+  emu::launch(blocks.Gcc.num_kn, blocks.Gcc.dim_kn, [&] { update_p(Lp.data(), _p0, _p, _phi, nu, dt, _phase); });
+  emu::launch(blocks.Gcc.num_kn, blocks.Gcc.dim_kn, [&] { copy_p_p_noghost(pm.data(), _p); });
+  real pmean = 0.;
+  for (long long c = 0; c < G.s3; c++) pmean += pm[c];
+  pmean /= (real)G.s3;
+  emu::launch(blocks.Gcc.num_kn, blocks.Gcc.dim_kn, [&] { forcing_add_c_const(-pmean, _p); });
+  memcpy(phi_b, _phi, sizeof(real) * G.s3b);
+  memcpy(u, _u, sizeof(real) * d.Gfx.s3b);
+  memcpy(v, _v, sizeof(real) * d.Gfy.s3b);
+  memcpy(w, _w, sizeof(real) * d.Gfz.s3b);
+  memcpy(p, _p, sizeof(real) * G.s3b);
+  return 0;
+}
+
+// sizes of the ghosted arrays: Gcc, Gfx, Gfy, Gfz s3b
+extern "C" void ref_sizes(long long *out) {
+  out[0] = dom[0].Gcc.s3b;
+  out[1] = dom[0].Gfx.s3b;
+  out[2] = dom[0].Gfy.s3b;
+  out[3] = dom[0].Gfz.s3b;
+}
+
+// the face flags and phase the harness built (for the other implementations)
+extern "C" void ref_flags(int *fu, int *fv, int *fw, int *phase) {
+  memcpy(fu, _flag_u, sizeof(int) * dom[0].Gfx.s3b);
+  memcpy(fv, _flag_v, sizeof(int) * dom[0].Gfy.s3b);
+  memcpy(fw, _flag_w, sizeof(int) * dom[0].Gfz.s3b);
+  memcpy(phase, _phase, sizeof(int) * dom[0].Gcc.s3b);
 }

@@ -18,6 +18,8 @@ int rank = 0, nprocs = 1, NPARTS = 0, nparts = 0, stepnum = 1, pp_max_iter = 200
 bb_real rho_f = 1.0, dt = 1.0, pp_residual = 1e-8;
 bb_real *_phi = 0, *_rhs_p = 0, *_invM = 0, *_u_star = 0, *_v_star = 0, *_w_star = 0;
 int *_phase = 0;
+bb_real *_u = 0, *_v = 0, *_w = 0, *_p = 0, *_p0 = 0; /* the epilogue's fields */
+int *_flag_u = 0, *_flag_v = 0, *_flag_w = 0;
 
 int stub_niter = -1, stub_calls = 0, stub_timed_calls = 0, stub_init_timed = 0;
 bb_real stub_resid = -1, stub_etime = -1, stub_spmv = -1, stub_up1 = -1;

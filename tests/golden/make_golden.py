@@ -38,6 +38,8 @@ def load():
     L.ref_invm.argtypes = [v]
     L.ref_rhs.argtypes = [ctypes.c_double, ctypes.c_double, v, v, v, v]
     L.ref_solve_u.argtypes = [ctypes.c_double, ctypes.c_double, v, v, v, ctypes.c_double, ctypes.c_int, v, v, v]
+    L.ref_epilogue.argtypes = [ctypes.c_double] * 3 + [v] * 10
+    L.ref_sizes.argtypes = [v]
     return L
 
 
@@ -166,6 +168,41 @@ def main():
         manifest[name] = {"kind": "dropin", "dims": dims, "bc": bc, "pp_residual": resid, "niter": it.value,
                           "resid": rs.value}
         print(name, it.value, rs.value)
+    # the time loop's steps after the solve: phi ghosts, projection, pressure update
+    import layout
+    epi_cases = [
+        ("epilogue_ppn_spheres", (12, 10, 8), (P, P, P, P, N, N), 3),
+        ("epilogue_nnp_noparts", (9, 11, 7), (N, N, N, N, P, P), 0),
+    ]
+    for name, dims, bc, nsph in epi_cases:
+        nx, ny, nz = dims
+        h = (1 / nx, 1.2 / ny, 0.9 / nz)
+        mask = None
+        if nsph:
+            cents = rng.random((nsph, 3))
+            cents[:, 2] = 0.25 + 0.5 * cents[:, 2]
+            mask = spheres_mask(dims, h, bc, cents, np.full(nsph, 0.2))
+        setup(L, dims, h, bc, mask)
+        phi = rng.normal(size=(nz, ny, nx))
+        us = rng.normal(size=(nz, ny, nx + 1))
+        vs = rng.normal(size=(nz, ny + 1, nx))
+        ws = rng.normal(size=(nz + 1, ny, nx))
+        p0 = rng.normal(size=(nz, ny, nx))
+        sz = np.zeros(4, np.int64)
+        L.ref_sizes(sz.ctypes.data)
+        ub, vb, wb = np.zeros(sz[1]), np.zeros(sz[2]), np.zeros(sz[3])
+        phib, pb = np.zeros(sz[0]), np.zeros(sz[0])
+        usb, vsb, wsb, p0b = layout.fx_to_s3b(us), layout.fy_to_s3b(vs), layout.fz_to_s3b(ws), layout.cells_to_s3b(p0)
+        assert (usb.size, vsb.size, wsb.size, p0b.size) == tuple(int(v) for v in (sz[1], sz[2], sz[3], sz[0]))
+        L.ref_epilogue(1.3, 0.02, 0.5, phi.ctypes.data, usb.ctypes.data, vsb.ctypes.data, wsb.ctypes.data,
+                       p0b.ctypes.data, phib.ctypes.data, ub.ctypes.data, vb.ctypes.data, wb.ctypes.data,
+                       pb.ctypes.data)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), dims=dims, h=h, bc=bc, rho_f=1.3, dt=0.02, nu=0.5,
+                            mask=mask if mask is not None else np.zeros(0, np.uint8), phi=phi, us=us, vs=vs, ws=ws,
+                            p0=p0, u=layout.fx_from_s3b(ub, dims), v=layout.fy_from_s3b(vb, dims),
+                            w=layout.fz_from_s3b(wb, dims), p=layout.cells_from_s3b(pb, dims), phi_b=phib)
+        manifest[name] = {"kind": "epilogue", "dims": dims, "bc": bc}
+        print(name)
     json.dump(manifest, open(os.path.join(HERE, "manifest.json"), "w"), indent=1)
 
 

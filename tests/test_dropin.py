@@ -117,6 +117,28 @@ def phase_b(mask, bc):
     return ph
 
 
+def flags_b(mask, bc, dims):
+    """Face flags in the reference's ghosted face layouts, by the rule the
+    host pin builds them with (cage_flag_*: -1 on a fluid/solid face;
+    flag_external_*: 0 on the wall faces of a non-periodic direction; else 1)."""
+    nx, ny, nz = dims
+    ph = phase_b(mask if mask is not None else np.zeros((nz, ny, nx), np.uint8), bc)
+    fl = ph < 0
+    U = np.ones((nx + 3, nz + 2, ny + 2), np.int32)   # [I, K, J]
+    U[1:nx + 2] = np.where(fl[:, :, :-1] != fl[:, :, 1:], -1, 1).transpose(2, 0, 1)
+    if bc[0] != 0:
+        U[1], U[nx + 1] = 0, 0
+    V = np.ones((ny + 3, nx + 2, nz + 2), np.int32)   # [J, I, K]
+    V[1:ny + 2] = np.where(fl[:, :-1, :] != fl[:, 1:, :], -1, 1).transpose(1, 2, 0)
+    if bc[2] != 0:
+        V[1], V[ny + 1] = 0, 0
+    W = np.ones((nz + 3, ny + 2, nx + 2), np.int32)   # [K, J, I]
+    W[1:nz + 2] = np.where(fl[:-1] != fl[1:], -1, 1)
+    if bc[4] != 0:
+        W[1], W[nz + 1] = 0, 0
+    return U, V, W
+
+
 def load(name):
     d = dict(np.load(os.path.join(GOLD, name + ".npz")))
     d["dims"] = tuple(int(x) for x in d["dims"])
@@ -153,7 +175,7 @@ def test_dropin_exports():
                          check=True).stdout
     syms = {l.split()[-1] for l in out.splitlines() if l.strip()}
     for s in ("cuda_PP_init_jacobi_preconditioner", "cuda_PP_cg", "cuda_PP_cg_noparts", "cuda_PP_cg_timed",
-              "bbpp_bluebottle_release"):
+              "cuda_dom_BC_p", "cuda_project", "cuda_update_p", "bbpp_bluebottle_release"):
         assert s in syms
     und = subprocess.run(["nm", "-D", "-u", bbpp.DROPIN_LIBPATH], capture_output=True, text=True,
                          check=True).stdout
@@ -284,3 +306,98 @@ def test_dropin_max_iter_exits_like_reference(bbpp_lib):
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
     assert r.returncode == 1, r.stdout + r.stderr
     assert "did not converge" in r.stdout and "returned" not in r.stdout
+
+
+# ------------------------------------------------------------ epilogue ----
+EPI = sorted(k for k, v in json.load(open(os.path.join(GOLD, "manifest.json"))).items() if v["kind"] == "epilogue")
+REFLIB = os.path.join(ROOT, "oracle", "_ref", "libref.so")
+
+
+@pytest.mark.skipif(not os.path.exists(REFLIB), reason="host build of the reference not present")
+@pytest.mark.parametrize("dims,bc,frac", [((7, 6, 5), (0, 0, 0, 0, 2, 2), 0.2), ((6, 8, 4), (2,) * 6, 0.3),
+                                          ((5, 4, 6), (0,) * 6, 0.0)])
+def test_flags_helper_matches_reference_host(dims, bc, frac):
+    """The face flags the drop-in epilogue test gives the library are the
+    ones the reference's host pin builds."""
+    sys.path.insert(0, GOLD)
+    import make_golden
+    L = make_golden.load()
+    L.ref_flags.argtypes = [ctypes.c_void_p] * 4
+    nx, ny, nz = dims
+    rng = np.random.default_rng(nx * ny)
+    mask = (rng.random((nz, ny, nx)) < frac).astype(np.uint8) if frac else None
+    make_golden.setup(L, dims, (1 / nx, 1 / ny, 1 / nz), bc, mask)
+    U, V, W = flags_b(mask, bc, dims)
+    fu, fv, fw = (np.zeros(a.size, np.int32) for a in (U, V, W))
+    ph = np.zeros((nx + 2) * (ny + 2) * (nz + 2), np.int32)
+    L.ref_flags(fu.ctypes.data, fv.ctypes.data, fw.ctypes.data, ph.ctypes.data)
+    assert np.array_equal(fu, U.ravel()) and np.array_equal(fv, V.ravel()) and np.array_equal(fw, W.ravel())
+    m = mask if mask is not None else np.zeros((nz, ny, nx), np.uint8)
+    assert np.array_equal(ph, phase_b(m, bc).ravel())
+
+
+def periodic_ghosts(a, bc):
+    """The host's one-rank mpi_cuda_exchange_Gcc on a (nz+2, ny+2, nx+2) array."""
+    a = a.copy()
+    if bc[0] == 0:
+        a[:, :, 0], a[:, :, -1] = a[:, :, -2], a[:, :, 1]
+    if bc[2] == 0:
+        a[:, 0, :], a[:, -1, :] = a[:, -2, :], a[:, 1, :]
+    if bc[4] == 0:
+        a[0], a[-1] = a[-2], a[1]
+    return a
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", EPI)
+def test_dropin_epilogue_matches_reference(bbpp_lib, name):
+    """cuda_dom_BC_p(_phi), cuda_project(), cuda_update_p() after a solve, on
+    the reference's ghosted arrays: ghosts and u, v, w equal the reference's
+    kernels bit for bit; p to rounding (the mean is summed in another order)."""
+    sys.path.insert(0, GOLD)
+    import layout
+    d = load(name)
+    nx, ny, nz = d["dims"]
+    H = Host()
+    H.setup(dict(d, u=d["us"], v=d["vs"], w=d["ws"]), 1e-8)
+    bc = d["bc"]
+    # phi with the host's periodic exchange done, as the time loop has it
+    phib = np.zeros((nz + 2, ny + 2, nx + 2))
+    phib[1:-1, 1:-1, 1:-1] = d["phi"]
+    phib = periodic_ghosts(phib, bc)
+    pptr = H.dev(phib.ravel())
+    H.g("_phi", ctypes.c_void_p).value = pptr
+    H.lib.cuda_dom_BC_p(ctypes.c_void_p(pptr))
+    got = np.empty(phib.size)
+    H.bbpp.lib().bbpp_sync()
+    H.bbpp.lib().bbpp_d2h(got.ctypes.data, pptr, got.nbytes)
+    assert np.array_equal(got, d["phi_b"])
+    # projection
+    U, V, W = flags_b(d["mask"], bc, d["dims"])
+    for nm, a in (("_flag_u", U), ("_flag_v", V), ("_flag_w", W)):
+        H.g(nm, ctypes.c_void_p).value = H.dev(np.ascontiguousarray(a.ravel()))
+    outs = {}
+    for nm, size in (("_u", U.size), ("_v", V.size), ("_w", W.size)):
+        outs[nm] = H.dev(np.zeros(size))
+        H.g(nm, ctypes.c_void_p).value = outs[nm]
+    H.lib.cuda_project()
+    H.bbpp.lib().bbpp_sync()
+    for nm, conv, ref in (("_u", layout.fx_from_s3b, d["u"]), ("_v", layout.fy_from_s3b, d["v"]),
+                          ("_w", layout.fz_from_s3b, d["w"])):
+        size = {"_u": U.size, "_v": V.size, "_w": W.size}[nm]
+        b = np.empty(size)
+        H.bbpp.lib().bbpp_d2h(b.ctypes.data, outs[nm], b.nbytes)
+        assert np.array_equal(conv(b, d["dims"]), ref)
+    # pressure update
+    if d["mask"] is None:
+        ph = phase_b(np.zeros((nz, ny, nx), np.uint8), bc)
+        H.g("_phase", ctypes.c_void_p).value = H.dev(np.ascontiguousarray(ph.ravel()))
+    H.g("_p0", ctypes.c_void_p).value = H.dev(layout.cells_to_s3b(d["p0"]))
+    pp = H.dev(np.zeros(phib.size))
+    H.g("_p", ctypes.c_void_p).value = pp
+    H.lib.cuda_update_p()
+    H.bbpp.lib().bbpp_sync()
+    b = np.empty(phib.size)
+    H.bbpp.lib().bbpp_d2h(b.ctypes.data, pp, b.nbytes)
+    p = layout.cells_from_s3b(b, d["dims"])
+    assert np.abs(p - d["p"]).max() <= 1e-14 * np.abs(d["p"]).max()

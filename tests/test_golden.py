@@ -96,3 +96,17 @@ def test_gpu_solve_matches_reference(bbpp_lib, name):
     assert abs(rep.iters - int(d["niter"])) <= 1
     ref = d["phi"]
     assert np.linalg.norm(x - ref) <= 1e-10 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("name", names("epilogue"))
+def test_oracle_epilogue_matches_reference(orc, name):
+    """Ghosts of phi, projection and pressure update after the solve: the
+    oracle's restatement against the reference's kernels (bit for bit; both
+    evaluate the same expressions in the same order without contraction)."""
+    d = load(name)
+    g = orc.grid(*d["dims"], *d["h"], bc=d["bc"])
+    u, v, w, p = orc.epilogue(g, d["mask"], float(d["rho_f"]), float(d["dt"]), d["phi"], d["us"], d["vs"], d["ws"],
+                              d["p0"])
+    for mine, ref in ((u, d["u"]), (v, d["v"]), (w, d["w"]), (p, d["p"])):
+        assert mine.shape == ref.shape
+        assert np.array_equal(mine, ref)
