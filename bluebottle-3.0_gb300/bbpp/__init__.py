@@ -111,6 +111,7 @@ def lib():
         "bbpp_solve_host": (I, [P, P, P, P, ctypes.POINTER(Opts), ctypes.POINTER(Report)]),
         "bbpp_spmv": (I, [P, P, P, P]),
         "bbpp_invm": (I, [P, P]),
+        "bbpp_rhs_div": (I, [P, D, D, P, P, P, P]),
         "bbpp_search_step": (I, [P, I, I, P, P, P, P, P, P, D, D, I, I, ctypes.POINTER(D)]),
         "bbpp_residual": (I, [P, P, P, P, P, ctypes.POINTER(D), ctypes.POINTER(D)]),
         "bbpp_sphere_mask": (I, [P, D, D, D, I, P, P, P, P, P]),
@@ -264,6 +265,10 @@ class Solver:
                                       _ptr(Ap), _ptr(x), beta, alpha, int(first), int(lag), ctypes.byref(pAp)),
                self.handle)
         return pAp.value
+
+    def rhs_div(self, rho_f, dt, u, v, w, out):
+        """rhs = -(rho_f/dt) div u* from dense face DeviceArrays (the reference's PP_rhs)."""
+        _check(lib().bbpp_rhs_div(self.handle, rho_f, dt, _ptr(u), _ptr(v), _ptr(w), _ptr(out)), self.handle)
 
     def invm(self, out):
         _check(lib().bbpp_invm(self.handle, _ptr(out)), self.handle)

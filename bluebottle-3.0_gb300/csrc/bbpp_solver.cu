@@ -873,6 +873,36 @@ extern "C" int bbpp_invm(bbpp_ctx *ctx, double *invM) {
   return 0;
 }
 
+// PP_rhs (src/solver_kernel.cu:152-173) on dense face arrays: rhs = -(rho/dt)
+// div u*, the reference's evaluation order without contraction.
+__global__ void k_rhs_div(int nx, int ny, int nz, double idx, double idy, double idz, double rho_idt,
+                          const double *__restrict__ u, const double *__restrict__ v, const double *__restrict__ w,
+                          double *__restrict__ rhs) {
+  const long long n = (long long)nx * ny * nz;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % nx);
+    const long long r = c / nx;
+    const int j = (int)(r % ny), k = (int)(r / ny);
+    const long long uw = i + (long long)(nx + 1) * (j + (long long)ny * k);
+    const long long vs = i + (long long)nx * (j + (long long)(ny + 1) * k);
+    double s = __dmul_rn(__dsub_rn(u[uw + 1], u[uw]), idx);
+    s = __dadd_rn(s, __dmul_rn(__dsub_rn(v[vs + nx], v[vs]), idy));
+    s = __dadd_rn(s, __dmul_rn(__dsub_rn(w[c + (long long)nx * ny], w[c]), idz));
+    rhs[c] = -__dmul_rn(s, rho_idt);
+  }
+}
+
+extern "C" int bbpp_rhs_div(bbpp_ctx *ctx, double rho_f, double dt, const double *u, const double *v, const double *w,
+                            double *rhs) {
+  if (!ctx || !u || !v || !w || !rhs || !(dt != 0.0)) return BBPP_BAD_ARG;
+  const Geo &G = ctx->G;
+  k_rhs_div<<<ctx->egrid, NT, 0, ctx->stream>>>(G.nx, G.ny, G.nz, 1. / ctx->grid.dx, 1. / ctx->grid.dy,
+                                                 1. / ctx->grid.dz, rho_f / dt, u, v, w, rhs);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
 // One search-kernel launch on caller vectors (kernel-level checks).
 template <typename T>
 static int search_once(bbpp_ctx *ctx, int kernel, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap,

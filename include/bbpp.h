@@ -132,6 +132,11 @@ int bbpp_solve_host(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, doubl
 /* Kernel-level entry points (device pointers), used for parity checks. */
 int bbpp_spmv(bbpp_ctx *ctx, const uint8_t *mask, const double *p, double *Ap);
 int bbpp_invm(bbpp_ctx *ctx, double *invM);
+/* The pressure right-hand side from the intermediate velocity, as PP_rhs (src/solver_kernel.cu:89-176):
+ * rhs = -(rho_f/dt) div(u*, v*, w*) on every cell.  Dense device arrays: faces
+ * u[i + (nx+1)(j + ny k)], v[i + nx(j + (ny+1) k)], w[i + nx(j + ny k)] (k = 0..nz); rhs as the cells. */
+int bbpp_rhs_div(bbpp_ctx *ctx, double rho_f, double dt, const double *u, const double *v, const double *w,
+                 double *rhs);
 /* One launch of the PCG search kernel on caller vectors, on the scaled operator L = S(-A) with
  * S = 1 / (2/dx^2 + 2/dy^2 + 2/dz^2) (kernel-level checks; no counterpart in the reference, whose
  * PP_update_search + PP_spmv_shared_load + (p, Ap) in src/solver_kernel.cu:528-713,906-927 it fuses).
