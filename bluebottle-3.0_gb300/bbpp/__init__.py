@@ -130,6 +130,7 @@ def lib():
         "bbpp_rng_gauss": (None, [ctypes.c_ulonglong, ctypes.c_longlong, P]),
         "bbpp_version": (ctypes.c_char_p, []),
         "bbpp_set_device": (I, [I]),
+        "bbpp_debug_wait": (I, [P, ctypes.c_longlong, I]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -60,7 +60,8 @@ struct DevState {
   int rep_maxgap;
   int last_rep;
   int rep_now;
-  int pad2;
+  int inject;            // test hook: 1 = the first TMA search CTA skips the copies of one plane
+  long long wait_ns;     // bound of a device-side wait (0: one second)
 };
 
 // Set by the last CTA of a search kernel: does this iteration's checkpoint

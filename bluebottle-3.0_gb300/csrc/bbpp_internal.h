@@ -85,6 +85,8 @@ struct bbpp_ctx {
   NetWork *net = nullptr;
   bbpp_tma_state *tma = nullptr;  // launch shape and tensor maps of the TMA search kernel
   bool pdl = false;               // iteration kernels launch with a programmatic dependency
+  int inject = 0;                 // test hook of bbpp_debug_wait (see DevState::inject)
+  long long wait_ns = 0;          // bound of device-side waits (0: one second)
 };
 
 // Launch an iteration kernel on ctx->stream; with ctx->pdl it may start while

@@ -72,6 +72,8 @@ static int solve_reliable(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs,
   hst->rep_d2 = o->ir_drop * o->ir_drop;
   hst->rep_maxgap = 8 * o->replace_every;
   hst->max_iter = o->max_iter;
+  hst->inject = ctx->inject;
+  hst->wait_ns = ctx->wait_ns;
   hst->stop = o->stop;
   hst->first = 1;
   CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));

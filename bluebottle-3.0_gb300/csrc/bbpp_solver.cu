@@ -732,6 +732,8 @@ int bbpp_pcg_init(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
   hst->tiny = (bscale == 1.0) ? 2.2250738585072014e-308 : 1e-16;
   t_bscale = bscale;
   hst->max_iter = max_iter;
+  hst->inject = ctx->inject;
+  hst->wait_ns = ctx->wait_ns;
   hst->stop = stop;
   hst->first = 1;
   CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
@@ -903,6 +905,16 @@ extern "C" int bbpp_rhs_div(bbpp_ctx *ctx, double rho_f, double dt, const double
   return 0;
 }
 
+// Failure-detection test hook: the bound of device-side waits, and whether the
+// next solves' TMA search kernel leaves one plane's copies unissued (its wait
+// then runs out and the solve returns BBPP_WAIT_TIMEOUT; no fault, no hang).
+extern "C" int bbpp_debug_wait(bbpp_ctx *ctx, long long wait_ns, int inject) {
+  if (!ctx || wait_ns < 0) return BBPP_BAD_ARG;
+  ctx->wait_ns = wait_ns;
+  ctx->inject = inject ? 1 : 0;
+  return 0;
+}
+
 // One search-kernel launch on caller vectors (kernel-level checks).
 template <typename T>
 static int search_once(bbpp_ctx *ctx, int kernel, const uint8_t *mask, const T *r, const T *pold, T *pnew, T *Ap,
@@ -942,6 +954,8 @@ extern "C" int bbpp_search_step(bbpp_ctx *ctx, int precision, int kernel, const 
   hst->alpha = alpha;
   hst->dlag = lag ? 1 : 0;
   hst->rz = 1.0;  // the kernel leaves alpha = rz / (p, Ap)
+  hst->inject = ctx->inject;
+  hst->wait_ns = ctx->wait_ns;
   CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
   int rc;
   if (precision == BBPP_FP64)

@@ -19,10 +19,12 @@
 // PP_spmv_shared_load + thrust (p, Ap) (src/solver_kernel.cu:528-713,906-927,
 // src/cuda_solver.cu:201-205,256-263), in FP32.
 //
-// Every mbarrier wait is bounded (about one second of globaltimer); a wait
-// that runs out marks the CTA, which keeps to the barrier schedule, drains its
-// outstanding copies with bounded waits, and ends the solve with
-// DONE_TIMEOUT for the host to report.
+// Every mbarrier wait is bounded (one second of globaltimer, or the state's
+// wait_ns); a wait that runs out marks the CTA, which keeps to the barrier
+// schedule, drains its outstanding copies with bounded waits, and ends the
+// solve with DONE_TIMEOUT for the host to report.  A test hook (inject) makes
+// one CTA leave one plane's copies unissued, so that this path runs without
+// any fault.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -69,13 +71,13 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-// Wait for the phase with this parity; false after ~1 s without completion.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned int parity) {
+// Wait for the phase with this parity; false after limit_ns without completion.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned int parity, unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer();
   for (unsigned int k = 1;; k++) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((k & 255u) == 0 && globaltimer() - t0 > 1000000000ull) return false;
+    if ((k & 255u) == 0 && globaltimer() - t0 > limit_ns) return false;
   }
 }
 
@@ -129,6 +131,11 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   const float beta = first ? 0.f : (float)(*(volatile double *)&st->beta);
   const bool lag = !first && *(volatile int *)&st->dlag;
   const float alpha = lag ? (float)(*(volatile double *)&st->alpha) : 0.f;
+  const long long wl = *(volatile long long *)&st->wait_ns;
+  const unsigned long long limit = wl > 0 ? (unsigned long long)wl : 1000000000ull;
+  // test hook: CTA (0,0) leaves one plane's copies unissued, so that its wait
+  // for them runs out and the solve ends with DONE_TIMEOUT
+  const bool skip_one = *(volatile int *)&st->inject && blockIdx.x == 0 && blockIdx.y == 0;
   load_tabs<float>(G, s_dL, s_inv);
 
   const int tid = threadIdx.x, lane = tid & 31;
@@ -152,6 +159,7 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   __syncthreads();
 
   auto issue = [&](int j) {  // thread 0: copies of plane z0-1+j into its stage
+    if (skip_one && j == 2) return;
     const int s = j % ns;
     int zr = z0 - 1 + j;
     if (G.pz) zr = (zr + nz) % nz;  // else -1 / nz read the zero fill
@@ -173,7 +181,7 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   // p_new over a stage, in place of r
   auto prep = [&](int j) {
     const int s = j % ns;
-    if (!mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u)) bad = true;
+    if (!mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u, limit)) bad = true;
     float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)s * 2 * arr);
     const float4 *ps = reinterpret_cast<const float4 *>(stage + (size_t)s * 2 * arr + arr);
     int zr = z0 - 1 + j;
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   if (__syncthreads_or(bad)) {
     // drain: every stage's last issued copy, with bounded waits
     if (tid == 0) {
-      for (int j = max(0, np - ns); j < np; j++) mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u);
+      for (int j = max(0, np - ns); j < np; j++) mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u, limit);
       atomicExch(&st->done, (int)DONE_TIMEOUT);
     }
     return;

@@ -245,6 +245,11 @@ void bbpp_rng_gauss(unsigned long long seed, long long n, double *out);
 
 /* Library version string. */
 const char *bbpp_version(void);
+/* Failure-detection test hook (no counterpart in the reference): set the bound of the solver's device-side
+ * waits (wait_ns > 0; 0 restores one second) and, with inject, make the next FP32 solves' TMA search kernel
+ * leave one plane's copies unissued in its first CTA, so that the wait for them runs out and the solve
+ * returns BBPP_WAIT_TIMEOUT.  Nothing faults or hangs; the context stays usable. */
+int bbpp_debug_wait(bbpp_ctx *ctx, long long wait_ns, int inject);
 /* Select the GPU for this host thread's later contexts and buffers (one process per GPU; no counterpart in
  * the reference, whose ranks each own one GPU through cudaSetDevice in its start-up code). */
 int bbpp_set_device(int device);
