@@ -51,6 +51,6 @@ def test_search_step_reports_wait_timeout(bbpp_lib):
     L.bbpp_debug_wait(s.handle, 1_000_000, 1)
     with pytest.raises(bbpp.BbppError) as e:
         s.search_step(r, r, z, z, z, m, first=True, precision=bbpp.FP32_IR, kernel=2)
-    assert e.value.args[0] == bbpp.WAIT_TIMEOUT
+    assert e.value.status == bbpp.WAIT_TIMEOUT
     L.bbpp_debug_wait(s.handle, 0, 0)
     s.search_step(r, r, z, z, z, m, first=True, precision=bbpp.FP32_IR, kernel=2)   # usable again
