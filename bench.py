@@ -310,7 +310,8 @@ def run_ours(args):
             assert rep.status == bbpp.CONVERGED
         bbpp.sync()
         prof(False)
-        print(json.dumps({"only": args.only, "iters": rep.iters, "ms": rep.ms, "launches": rep.launches}))
+        print(json.dumps({"only": args.only, "iters": rep.iters, "ms": rep.ms, "guess_ms": rep.guess_ms,
+                          "launches": rep.launches}))
         return
 
     for name, kw in methods.items():

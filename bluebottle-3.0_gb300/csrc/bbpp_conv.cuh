@@ -7,7 +7,8 @@
 // on the axes flagged periodic and zero otherwise.
 //
 //  k_conv3_fwd<CIN, COUT>   out = act(conv(in, W) + bias); a CTA computes a
-//                           16x8x2 tile of outputs from a halo tile staged in
+//                           16x8xTZ tile of outputs (TZ = 4 for up to 32
+//                           output channels, else 2) from a halo tile staged in
 //                           shared memory 16 input channels at a time; the 27
 //                           taps are 27 k16 steps whose A rows are shifted
 //                           halo rows (ldmatrix gather).  dgrad uses the same
@@ -84,30 +85,40 @@ __device__ __forceinline__ bool pad_axis(int &g, int n, int periodic) {
 }
 
 // ------------------------------------------------------------- forward -----
+// z planes of the forward kernel's output tile: deeper tiles reuse every
+// weight fragment over more A fragments and cut the halo share, as long as
+// the accumulators fit in registers
+template <int COUT>
+__host__ __device__ constexpr int fwd_tz() {
+  return COUT <= 32 ? 4 : 2;
+}
+
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(256) k_conv3_fwd(const ConvArgs a) {
   static_assert(CIN % 16 == 0 && COUT % 16 == 0, "channels in multiples of 16");
+  constexpr int TZ = fwd_tz<COUT>();
+  constexpr int HVZ = HTX * HTY * (TZ + 2);  // halo voxels
   extern __shared__ __align__(16) unsigned char smem[];
-  unsigned char *s_in = smem;              // HVOX rows of RSB bytes
-  unsigned char *s_w = smem + HVOX * RSB;  // 27 * COUT rows of RSB bytes
+  unsigned char *s_in = smem;              // HVZ rows of RSB bytes
+  unsigned char *s_w = smem + HVZ * RSB;   // 27 * COUT rows of RSB bytes
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int x0 = blockIdx.x * CTX, y0 = blockIdx.y * CTY;
-  const int nzt = (a.nz + CTZ - 1) / CTZ;
+  const int nzt = (a.nz + TZ - 1) / TZ;
   const int vb = blockIdx.z / nzt;
-  const int z0 = (blockIdx.z - vb * nzt) * CTZ;
+  const int z0 = (blockIdx.z - vb * nzt) * TZ;
   const long long vol = (long long)a.nx * a.ny * a.nz;
   const bf16 *inb = a.in + (long long)vb * vol * a.ldi + a.ci_off;
 
-  float acc[CTZ][COUT / 8][4];
+  float acc[TZ][COUT / 8][4];
 #pragma unroll
-  for (int i = 0; i < CTZ; i++)
+  for (int i = 0; i < TZ; i++)
 #pragma unroll
     for (int j = 0; j < COUT / 8; j++)
 #pragma unroll
       for (int q = 0; q < 4; q++) acc[i][j][q] = 0.f;
 
   for (int c0 = 0; c0 < CIN; c0 += 16) {
-    for (int idx = tid; idx < HVOX * 2; idx += 256) {
+    for (int idx = tid; idx < HVZ * 2; idx += 256) {
       const int e = idx >> 1, half = idx & 1;
       const int hx = e % HTX, t = e / HTX;
       const int hy = t % HTY, hz = t / HTY;
@@ -133,7 +144,7 @@ __global__ void __launch_bounds__(256) k_conv3_fwd(const ConvArgs a) {
         ldsm_x4(bfr[j][0], bfr[j][1], bfr[j + 1][0], bfr[j + 1][1], s_w + n * RSB + ((lane >> 3) & 1) * 16);
       }
 #pragma unroll
-      for (int mi = 0; mi < CTZ; mi++) {
+      for (int mi = 0; mi < TZ; mi++) {
         uint32_t afr[4];
         const int hv = ((mi + dz) * HTY + warp + dy) * HTX + (lane & 15) + dx;
         ldsm_x4(afr[0], afr[1], afr[2], afr[3], s_in + hv * RSB + (lane >> 4) * 16);
@@ -148,7 +159,7 @@ __global__ void __launch_bounds__(256) k_conv3_fwd(const ConvArgs a) {
   if (y >= a.ny) return;
   bf16 *outb = a.out + (long long)vb * vol * a.ldo + a.co_off;
 #pragma unroll
-  for (int mi = 0; mi < CTZ; mi++) {
+  for (int mi = 0; mi < TZ; mi++) {
     const int z = z0 + mi;
     if (z >= a.nz) continue;
 #pragma unroll
@@ -175,8 +186,8 @@ __global__ void __launch_bounds__(256) k_conv3_fwd(const ConvArgs a) {
 }
 
 template <int CIN, int COUT>
-constexpr int conv_fwd_smem() {
-  return HVOX * RSB + 27 * COUT * RSB;
+__host__ __device__ constexpr int conv_fwd_smem() {
+  return HTX * HTY * (fwd_tz<COUT>() + 2) * RSB + 27 * COUT * RSB;
 }
 
 // --------------------------------------------------------------- wgrad -----

@@ -57,7 +57,8 @@ cudaError_t conv_fwd_t(const ConvArgs &a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dim3 grid((a.nx + CTX - 1) / CTX, (a.ny + CTY - 1) / CTY, a.nb * ((a.nz + CTZ - 1) / CTZ));
+  constexpr int TZ = fwd_tz<COUT>();
+  dim3 grid((a.nx + CTX - 1) / CTX, (a.ny + CTY - 1) / CTY, a.nb * ((a.nz + TZ - 1) / TZ));
   k_conv3_fwd<CIN, COUT><<<grid, 256, smem, s>>>(a);
   return cudaGetLastError();
 }
