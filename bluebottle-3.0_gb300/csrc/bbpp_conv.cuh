@@ -7,8 +7,8 @@
 // on the axes flagged periodic and zero otherwise.
 //
 //  k_conv3_fwd<CIN, COUT>   out = act(conv(in, W) + bias); a CTA computes a
-//                           16x8xTZ tile of outputs (TZ = 4 for up to 32
-//                           output channels, else 2) from a halo tile staged in
+//                           16x8xTZ tile of outputs (TZ = 8, 4, 2 for 16,
+//                           32, 64 output channels) from a halo tile staged in
 //                           shared memory 16 input channels at a time; the 27
 //                           taps are 27 k16 steps whose A rows are shifted
 //                           halo rows (ldmatrix gather).  dgrad uses the same
@@ -90,7 +90,7 @@ __device__ __forceinline__ bool pad_axis(int &g, int n, int periodic) {
 // the accumulators fit in registers
 template <int COUT>
 __host__ __device__ constexpr int fwd_tz() {
-  return COUT <= 32 ? 4 : 2;
+  return COUT <= 16 ? 8 : (COUT <= 32 ? 4 : 2);
 }
 
 template <int CIN, int COUT>

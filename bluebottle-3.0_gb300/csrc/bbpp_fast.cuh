@@ -22,6 +22,8 @@
 //  k_resid_s  r = bscale rhs - L x (solid cells 0) with (r,z), (r,r), (rhs,rhs).
 #pragma once
 
+#include <type_traits>
+
 #include "bbpp_dev.cuh"
 
 namespace bbpp {
@@ -566,14 +568,16 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       sm[slot][ly][lx] = m;
     }
   };
-  double rz = 0, rr = 0, bb = 0;
+  // (r,z) = (r,r) + sum over wall cells of (invL - 1) r^2; (rhs,rhs) only
+  // when initialising.  Both are CTA-uniform choices, so the FP64 pipe sees
+  // no predicated work on interior planes (FP64 issues at 1/64 of FP32).
+  double corr = 0, rr = 0, bb = 0;
+  const bool want_bb = mode == 0;
   load_plane(0, z0 - 1);
   load_plane(1, z0);
   const int gx = x0 + tx;
-  for (int z = z0; z < z1; z++) {
-    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
-    load_plane(st_, z + 1);
-    __syncthreads();
+  auto cell = [&](auto interior_tag, int sb, int sc, int st_, int z) {
+    constexpr bool INTERIOR = decltype(interior_tag)::value;
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       const int gy = y0 + ty + 8 * h;
@@ -582,7 +586,7 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       const bool mc = MASK && sm[sc][ly][lx] != 0;
       const long long c = gx + (long long)nx * gy + sxy * z;
       const TXT bv = rhs[c];
-      bb = fma((double)bv, (double)bv, bb);
+      if (want_bb) bb = fma((double)bv, (double)bv, bb);
       if (mc) {
         rout[c] = TR(0);
         if (mode == 0) xin[c] = TXT(0);
@@ -592,18 +596,30 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       TXT pe = sp[sc][ly][lx + 1], pw = sp[sc][ly][lx - 1];
       TXT pn = sp[sc][ly + 1][lx], ps = sp[sc][ly - 1][lx];
       TXT pt = sp[st_][ly][lx], pb = sp[sb][ly][lx];
-      const int cls = wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py) + 9 * wall_count(z, nz, G.pz);
+      const int cls = INTERIOR ? 0 : wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py) + 9 * wall_count(z, nz, G.pz);
       const TXT a = apply_L<TXT, ISO>(G, s_dL, cls, pc, pe, pw, pn, ps, pt, pb);
       const TXT rv = fma((TXT)bscale, bv, -a);
       const TR ro = (TR)rv;
       rout[c] = ro;
       const double rd = (double)rv;
-      rr = fma(rd, rd, rr);
-      rz = fma(rd, (double)s_inv[cls] * rd, rz);
+      if (INTERIOR) {
+        rr = fma(rd, rd, rr);
+      } else {
+        const double r2 = rd * rd;
+        rr += r2;
+        if (cls) corr = fma((double)s_inv[cls] - 1.0, r2, corr);
+      }
     }
+  };
+  for (int z = z0; z < z1; z++) {
+    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
+    load_plane(st_, z + 1);
+    __syncthreads();
+    if (G.px && G.py && wall_count(z, nz, G.pz) == 0) cell(std::true_type(), sb, sc, st_, z);
+    else cell(std::false_type(), sb, sc, st_, z);
     __syncthreads();
   }
-  double v[3] = {rz, rr, bb}, tot[3];
+  double v[3] = {rr + corr, rr, bb}, tot[3];
   const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
   const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
   if (last_cta_reduce<3>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
