@@ -36,6 +36,8 @@ def _sig():
         "bbpp_conv3": (I, [I, I, P, I, I, P, P, P, I, I, I, I, I, I, I, I, I, I]),
         "bbpp_conv3_wgrad": (I, [I, I, P, I, I, P, I, P, I, I, I, I, I, I, I]),
         "bbpp_conv3_wflip": (I, [I, I, P, P]),
+        "bbpp_conv3_tc_launches": (ctypes.c_longlong, []),
+        "bbpp_conv3_tc_config": (I, [I, I]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

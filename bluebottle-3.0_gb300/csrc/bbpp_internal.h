@@ -49,6 +49,7 @@ struct IrBuffers;   // FP32 inner-sweep workspace (bbpp_ir.cu)
 struct NetWork;     // learned-guess workspace (bbpp_net.cu)
 
 struct bbpp_tma_state;
+void *bbpp_tensor_map_encoder();  // cuTensorMapEncodeTiled, or null
 
 struct bbpp_ctx {
   bbpp_grid grid{};

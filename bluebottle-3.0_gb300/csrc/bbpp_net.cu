@@ -21,17 +21,20 @@
 //   OUT = D1 . w_head + b_head  (FP32)
 // Loss: mean over fluid cells of (OUT - (p* - p_prev) s_r / h^2)^2.
 // Padding is periodic in x and y and zero in z (the workloads' boundaries).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
 #include "../../include/bbpp.h"
 #include "bbpp_conv.cuh"
+#include "bbpp_conv_tc.cuh"
 #include "bbpp_internal.h"
 
 using namespace bbnet;
@@ -63,7 +66,143 @@ cudaError_t conv_fwd_t(const ConvArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// tcgen05 path: error word of timed-out waits (bounded mbarrier waits)
+__device__ int g_tc_err;
+long long g_tc_launches = 0;  // tcgen05 convolutions launched by this process
+int g_tc_max_ctas = 0;        // > 0: cap on the persistent grid (tests: longer z marches per CTA)
+int g_tc_on = -1;             // -1: the environment decides (BBPP_CONV_TC=1 turns the kernel on)
+
+typedef CUresult (*TmEncode)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                             const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                             CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// tensor maps of one (input, weights) pair, cached: the network calls the
+// same few layers with the same buffers every time
+struct TmKey {
+  const void *in, *w;
+  int ldi, nx, ny, nz, nb, cin, cout;
+  bool operator==(const TmKey &o) const {
+    return in == o.in && w == o.w && ldi == o.ldi && nx == o.nx && ny == o.ny && nz == o.nz && nb == o.nb &&
+           cin == o.cin && cout == o.cout;
+  }
+};
+
+bool tm_build(const TmKey &k, int rows, TmMaps *m) {
+  TmEncode fn = reinterpret_cast<TmEncode>(bbpp_tensor_map_encoder());
+  if (!fn) return false;
+  const cuuint64_t e = 2;
+  const cuuint64_t dim[5] = {(cuuint64_t)k.ldi, (cuuint64_t)k.nx, (cuuint64_t)k.ny, (cuuint64_t)k.nz,
+                             (cuuint64_t)k.nb};
+  const cuuint64_t str[4] = {k.ldi * e, k.nx * k.ldi * e, (cuuint64_t)k.ny * k.nx * k.ldi * e,
+                             (cuuint64_t)k.nz * k.ny * k.nx * k.ldi * e};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  const cuuint32_t widths[3] = {144, 136, 128};
+  const cuuint32_t box[5] = {8, 144, (cuuint32_t)rows, 1, 1};
+  if (fn(&m->rows, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(k.in), dim, str, box, es,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  for (int i = 0; i < 3; i++) {
+    const cuuint32_t box1[5] = {8, widths[i], 1, 1, 1};
+    if (fn(&m->row[i], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(k.in), dim, str, box1, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return false;
+  }
+  const cuuint64_t wdim[3] = {(cuuint64_t)k.cin, (cuuint64_t)k.cout, 27};
+  const cuuint64_t wstr[2] = {k.cin * e, (cuuint64_t)k.cout * k.cin * e};
+  const cuuint32_t wbox[3] = {8, (cuuint32_t)k.cout, 27};
+  return fn(&m->w, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(k.w), wdim, wstr, wbox, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool tm_maps(const TmKey &k, int rows, TmMaps *out) {
+  static std::vector<std::pair<TmKey, TmMaps>> cache;
+  for (const auto &c : cache)
+    if (c.first == k) {
+      *out = c.second;
+      return true;
+    }
+  TmMaps m;
+  if (!tm_build(k, rows, &m)) return false;
+  if (cache.size() >= 32) cache.erase(cache.begin());
+  cache.emplace_back(k, m);
+  *out = m;
+  return true;
+}
+
+template <int CIN, int COUT>
+cudaError_t conv_tc_t(const ConvArgs &a, cudaStream_t s) {
+  constexpr int smem = tm_smem<CIN, COUT>();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static unsigned long long attr = 0;  // per device
+  if (dev < 64 && !(attr & (1ull << dev))) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3_tm<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr |= 1ull << dev;
+  }
+  TmKey key{a.in, a.w, a.ldi, a.nx, a.ny, a.nz, a.nb, CIN, COUT};
+  TmMaps maps;
+  if (!tm_maps(key, tm_tyr<COUT>() + 2, &maps)) return cudaErrorNotSupported;  // the caller falls back
+  TmGeo g;
+  g.nxb = a.nx / 128;
+  g.nyb = (a.ny + tm_tyr<COUT>() - 1) / tm_tyr<COUT>();
+  g.units = (long long)a.nb * g.nyb * g.nxb * a.nz;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int cap = std::max(sms, 1);
+  if (g_tc_max_ctas > 0) cap = std::min(cap, g_tc_max_ctas);
+  const int grid = (int)std::min<long long>(cap, g.units);
+  int *err = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  k_conv3_tm<CIN, COUT><<<grid, TM_THREADS, smem, s>>>(a, maps, g, err);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) g_tc_launches++;
+  return e;
+}
+
+// The tcgen05 kernel is off unless BBPP_CONV_TC=1 (or a test turns it on):
+// a tcgen05.mma of M = 128, K = 16 costs about 200 cycles whatever its N, and
+// these layers have N = 16 or 32 output channels per MMA, so the kernel runs
+// at ~150-250 TFLOP/s, no faster than the mma.sync kernel.
+bool conv_tc_enabled() {
+  if (g_tc_on < 0) {
+    const char *v = getenv("BBPP_CONV_TC");
+    return v && v[0] == '1';
+  }
+  return g_tc_on == 1;
+}
+
+// the tcgen05 kernel takes 128-voxel x blocks, 16-byte aligned channel runs and
+// tensor maps (a driver with cuTensorMapEncodeTiled)
+bool conv_tc_fits(const ConvArgs &a) {
+  const auto al16 = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+  return conv_tc_enabled() && a.nx % 128 == 0 && a.ldi % 8 == 0 && a.ci_off % 8 == 0 && a.ldo % 8 == 0 &&
+         a.co_off % 8 == 0 && al16(a.in) && al16(a.w) && al16(a.out) && bbpp_tensor_map_encoder() != nullptr;
+}
+
+// nonzero once a tcgen05 convolution gave up a wait; cleared by the read
+int conv_tc_failed() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tc_err, sizeof(int)) != cudaSuccess) return 1;
+  if (v) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_tc_err, &zero, sizeof(int));
+  }
+  return v;
+}
+
 cudaError_t conv_fwd(int cin, int cout, const ConvArgs &a, cudaStream_t s) {
+#define TCASE(CI, CO)                                     \
+  if (cin == CI && cout == CO && conv_tc_fits(a)) {         \
+    const cudaError_t e_ = conv_tc_t<CI, CO>(a, s);         \
+    if (e_ != cudaErrorNotSupported) return e_;             \
+  }
+  TCASE(16, 16) TCASE(16, 32) TCASE(96, 32) TCASE(48, 16) TCASE(32, 16)
+#undef TCASE
 #define CASE(CI, CO) \
   if (cin == CI && cout == CO) return conv_fwd_t<CI, CO>(a, s);
   CASE(16, 16) CASE(16, 32) CASE(32, 64) CASE(96, 32) CASE(48, 16)  // forward layers
@@ -946,6 +1085,19 @@ extern "C" int bbpp_conv3(int cin, int cout, const void *in, int ldi, int ci_off
   if (ldi % 8 || ci_off % 8 || ldo % 2 || co_off % 2 || nb < 1 || nx < 1 || ny < 1 || nz < 1) return BBPP_BAD_ARG;
   if (conv_fwd(cin, cout, a, 0) != cudaSuccess) return BBPP_BAD_ARG;
   NCK(cudaDeviceSynchronize());
+  if (conv_tc_failed()) return BBPP_WAIT_TIMEOUT;
+  return 0;
+}
+
+// Number of convolutions that ran on the tcgen05 kernel in this process.
+extern "C" long long bbpp_conv3_tc_launches(void) { return g_tc_launches; }
+
+// Kernel choice: enable (1) or disable (0) the tcgen05 kernel, or (-1) leave
+// the choice to BBPP_CONV_TC; and cap its persistent grid (0: one CTA per SM).
+extern "C" int bbpp_conv3_tc_config(int enable, int max_ctas) {
+  if (enable < -1 || enable > 1 || max_ctas < 0) return BBPP_BAD_ARG;
+  g_tc_on = enable;
+  g_tc_max_ctas = max_ctas;
   return 0;
 }
 
@@ -998,6 +1150,7 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
   n->stream = saved;
   if (rc == 0) {
     cudaEventSynchronize(e1);
+    if (conv_tc_failed()) rc = BBPP_WAIT_TIMEOUT;
     float t = 0.f;
     cudaEventElapsedTime(&t, e0, e1);
     if (ms) *ms = t;

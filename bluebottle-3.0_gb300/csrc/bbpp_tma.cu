@@ -416,6 +416,9 @@ int env_int(const char *name, int dflt) {
 
 }  // namespace
 
+// cuTensorMapEncodeTiled of the driver (null when the driver has none)
+void *bbpp_tensor_map_encoder() { return reinterpret_cast<void *>(encode_fn()); }
+
 struct bbpp_tma_state {
   bool ok = false;
   int ty = 0, npt = 0, ns = 0, kz = 0, four_d = 0, smem = 0;

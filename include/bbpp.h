@@ -238,6 +238,15 @@ int bbpp_conv3(int cin, int cout, const void *in, int ldi, int ci_off, const voi
 int bbpp_conv3_wgrad(int cin, int cout, const void *in, int ldi, int ci_off, const void *g, int ldg, float *dW,
                      int nx, int ny, int nz, int nb, int px, int py, int pz);
 int bbpp_conv3_wflip(int cin, int cout, const void *w, void *wt);
+/* Convolutions run so far on the tcgen05 (tensor-memory) kernel.  When it is
+ * enabled, forward layers with 16 or 32 outputs on 128-voxel x blocks take
+ * it; the others, and all layers when it is off (the default), take the
+ * mma.sync kernel. */
+long long bbpp_conv3_tc_launches(void);
+/* Enable (1) / disable (0) the tcgen05 kernel, or (-1) leave the choice to
+ * the environment (BBPP_CONV_TC=1 enables it); cap its persistent grid at
+ * max_ctas CTAs (0: one per SM). */
+int bbpp_conv3_tc_config(int enable, int max_ctas);
 
 /* Ranq1 generator (src/rng.c:25-107), for reproducible synthetic inputs. */
 void bbpp_rng_uniform(unsigned long long seed, long long n, double lo, double hi, double *out);

@@ -1,7 +1,8 @@
 """GPU checks of the learned initial guess.
 
-Kernel level: the BF16 tensor-core 3x3x3 convolution (forward, input gradient
-through the flipped weights, weight gradient) against torch's FP32 conv3d on
+Kernel level: the BF16 tensor-core 3x3x3 convolutions (forward on the
+mma.sync and tcgen05 kernels, input gradient through the flipped weights,
+weight gradient) against torch's FP32 conv3d on
 the same BF16 values, with periodic and zero padding and partial tiles.
 Network level: loss and gradient of the whole encoder-decoder against the
 FP32 CPU reference (oracle/net_oracle.py); training on the GPU lowers the
@@ -45,7 +46,10 @@ CONVS = [(16, 16), (16, 32), (32, 64), (96, 32), (48, 16)]
 
 
 @pytest.mark.parametrize("cin,cout", CONVS)
-@pytest.mark.parametrize("dims,pads", [((20, 12, 6), (1, 1, 0)), ((16, 8, 4), (0, 0, 0)), ((33, 9, 3), (1, 0, 1))])
+# rows of 128 voxels take the tcgen05 kernel (16 or 32 output channels) when it
+# is enabled, the others the mma.sync kernel
+@pytest.mark.parametrize("dims,pads", [((20, 12, 6), (1, 1, 0)), ((16, 8, 4), (0, 0, 0)), ((33, 9, 3), (1, 0, 1)),
+                                       ((128, 5, 3), (1, 1, 0)), ((256, 2, 5), (0, 1, 1))])
 def test_conv3_forward_dgrad_wgrad(bbpp_lib, cin, cout, dims, pads):
     L = learned._sig()
     nx, ny, nz = dims
@@ -58,8 +62,15 @@ def test_conv3_forward_dgrad_wgrad(bbpp_lib, cin, cout, dims, pads):
     dx, dw = dev_bf16(x), dev_bf16(w)
     db = bbpp.DeviceArray.from_host(bias)
     dy = bbpp.DeviceArray((nb, nz, ny, nx, cout), np.uint16)
-    assert L.bbpp_conv3(cin, cout, dx.ptr, cin, 0, dw.ptr, db.ptr, dy.ptr, cout, 0, nx, ny, nz, nb, px, py, pz,
-                        0) == 0
+    tc0 = L.bbpp_conv3_tc_launches()
+    assert L.bbpp_conv3_tc_config(1, 0) == 0
+    try:
+        assert L.bbpp_conv3(cin, cout, dx.ptr, cin, 0, dw.ptr, db.ptr, dy.ptr, cout, 0, nx, ny, nz, nb, px, py, pz,
+                            0) == 0
+    finally:
+        L.bbpp_conv3_tc_config(-1, 0)
+    # with the tcgen05 kernel enabled, the shapes it takes ran on it
+    assert L.bbpp_conv3_tc_launches() - tc0 == (1 if nx % 128 == 0 and cout in (16, 32) else 0)
     y = NO.bits_f32(dy.download())
     xt, wt = torch_conv(x, w, px, py, pz)
     xt.requires_grad_(True)
@@ -85,6 +96,45 @@ def test_conv3_forward_dgrad_wgrad(bbpp_lib, cin, cout, dims, pads):
     assert L.bbpp_conv3_wgrad(cin, cout, dx.ptr, cin, 0, dg.ptr, cout, dW.ptr, nx, ny, nz, nb, px, py, pz) == 0
     got_dw = dW.download()
     assert np.abs(got_dw - dw_ref).max() <= 2e-4 * np.abs(dw_ref).max()
+
+
+TC_CONVS = [(16, 16), (16, 32), (96, 32), (48, 16), (32, 16)]
+
+
+@pytest.mark.parametrize("cin,cout", TC_CONVS)
+@pytest.mark.parametrize("dims,pads,nb", [((256, 8, 10), (1, 1, 0), 1), ((128, 6, 12), (1, 1, 0), 2),
+                                          ((256, 5, 9), (0, 1, 1), 1)])
+@pytest.mark.parametrize("ctas", [1, 5])
+def test_conv3_tc_marching(bbpp_lib, cin, cout, dims, pads, nb, ctas):
+    """The tcgen05 kernel with few CTAs, so each marches through many planes
+    and tiles (accumulator ring reuse, segment changes, one- and two-sided
+    periodic x wrap), writing into a channel window of a wider output."""
+    L = learned._sig()
+    nx, ny, nz = dims
+    px, py, pz = pads
+    rng = np.random.default_rng(cin * 3 + cout + nx + ctas)
+    x = NO.bits_f32(NO.bf16_bits(rng.normal(size=(nb, nz, ny, nx, cin)).astype(np.float32)))
+    w = NO.bits_f32(NO.bf16_bits((rng.normal(size=(27, cout, cin)) * 0.1).astype(np.float32)))
+    bias = rng.normal(size=cout).astype(np.float32)
+    dx, dw = dev_bf16(x), dev_bf16(w)
+    db = bbpp.DeviceArray.from_host(bias)
+    ldo, co_off = cout + 16, 8
+    dy = bbpp.DeviceArray((nb, nz, ny, nx, ldo), np.uint16)
+    dy.zero()
+    tc0 = L.bbpp_conv3_tc_launches()
+    assert L.bbpp_conv3_tc_config(1, ctas) == 0
+    try:
+        assert L.bbpp_conv3(cin, cout, dx.ptr, cin, 0, dw.ptr, db.ptr, dy.ptr, ldo, co_off, nx, ny, nz, nb, px, py,
+                            pz, 1) == 0
+    finally:
+        L.bbpp_conv3_tc_config(-1, 0)
+    assert L.bbpp_conv3_tc_launches() - tc0 == 1
+    y = NO.bits_f32(dy.download())
+    xt, wt = torch_conv(x, w, px, py, pz)
+    yref = torch.relu(conv_ref(xt, wt, px, py, pz) + torch.as_tensor(bias).view(1, -1, 1, 1, 1))
+    yref = yref.permute(0, 2, 3, 4, 1).numpy()
+    assert np.abs(y[..., co_off:co_off + cout] - yref).max() <= 1e-2 * np.abs(yref).max()
+    assert not y[..., :co_off].any() and not y[..., co_off + cout:].any()  # channels outside the window untouched
 
 
 def _small_problem(seed, dims=(16, 16, 8), nb=2):
