@@ -285,10 +285,13 @@ def run_ours(args):
                "ir_every50": dict(precision=bbpp.FP32_IR, ir_drop=0.0),
                "ir_warm": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_GIVEN)}
     headline = "ir"
-    if not args.no_learned and args.only in (None, "learned_ir"):
+    if not args.no_learned and args.only in (None, "learned_ir", "learned_ir_fine"):
         net, net_info = train_c4_net(args)
         methods["learned_ir"] = dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle,
                                      prev=dprev.ptr)
+        # the same network run on the 256^3 grid itself instead of the grid restricted by 2
+        methods["learned_ir_fine"] = dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle,
+                                          prev=dprev.ptr, net_coarsen=1)
         headline = "learned_ir"
 
     def step(kw):
@@ -421,7 +424,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32-inner/f64-refined" if headline == "ir" else "f64",
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "method": {"ir": "FP32 Jacobi PCG with FP64 reliable updates",
-                                                     "learned_ir": "learned guess (C4 net) + FP32 Jacobi PCG with "
+                                                     "learned_ir": "learned guess (C4 net, run on the grid "
+                                                                   "restricted by 2) + FP32 Jacobi PCG with "
                                                                    "FP64 reliable updates",
                                                      "fp64": "plain FP64 Jacobi PCG"}[headline],
                    "l2": "flushed (512 MB write) before every step; working set 0.9 GB > L2",
@@ -460,7 +464,8 @@ def main():
     ap.add_argument("--net", default=None, help="load (or save after training) the learned-guess network here")
     ap.add_argument("--train-samples", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=1500)
-    ap.add_argument("--only", default=None, choices=["fp64", "ir", "ir_restart", "ir_every50", "ir_warm", "learned_ir"],
+    ap.add_argument("--only", default=None, choices=["fp64", "ir", "ir_restart", "ir_every50", "ir_warm", "learned_ir",
+                                                        "learned_ir_fine"],
                     help="run only warm-up + steps solves of one method (profiler runs)")
     ap.add_argument("--ref-iters", type=int, default=0,
                     help="iterations of a full solve for the reference arm (0: the measured C3 count)")

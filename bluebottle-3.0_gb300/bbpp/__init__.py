@@ -70,7 +70,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("guess", ctypes.c_int), ("stop", ctypes.c_int),
                 ("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("replace_every", ctypes.c_int),
                 ("inner_tol", ctypes.c_double), ("max_outer", ctypes.c_int),
-                ("net", ctypes.c_void_p), ("prev", ctypes.c_void_p), ("ir_mode", ctypes.c_int), ("ir_drop", ctypes.c_double)]
+                ("net", ctypes.c_void_p), ("prev", ctypes.c_void_p), ("ir_mode", ctypes.c_int), ("ir_drop", ctypes.c_double),
+                ("net_coarsen", ctypes.c_int)]
 
 
 class Report(ctypes.Structure):

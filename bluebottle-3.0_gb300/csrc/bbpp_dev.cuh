@@ -86,6 +86,36 @@ struct Geo {
   unsigned long long mx, mxy;
 };
 
+// L2 eviction priority of one access (createpolicy): 0 normal, 1 evict_first
+// (streamed data), 2 evict_last (data the next kernel reads again)
+__device__ __forceinline__ unsigned long long l2_policy(int kind) {
+  unsigned long long p;
+  if (kind == 2) asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  else if (kind == 1) asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  else asm volatile("createpolicy.fractional.L2::evict_normal.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+
+__device__ __forceinline__ float4 ld4_pol(const float4 *a, unsigned long long pol) {
+  float4 v;
+  asm("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(a), "l"(pol));
+  return v;
+}
+
+__device__ __forceinline__ void st4_pol(float4 *a, const float4 v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "f"(v.x), "f"(v.y), "f"(v.z),
+               "f"(v.w), "l"(pol)
+               : "memory");
+}
+
+__device__ __forceinline__ unsigned int ld_u32_pol(const void *a, unsigned long long pol) {
+  unsigned int v;
+  asm("ld.global.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+  return v;
+}
+
 __device__ __forceinline__ unsigned int fdiv(unsigned int n, unsigned long long m) {
   return m ? (unsigned int)__umul64hi((unsigned long long)n, m) : n;
 }

@@ -409,6 +409,12 @@ template <> struct Vec16<double> {
   static constexpr int E = 2;
 };
 
+// vector loads and stores with an L2 policy (FP32); FP64 vectors plain
+__device__ __forceinline__ float4 ldv(const float4 *a, unsigned long long pol) { return ld4_pol(a, pol); }
+__device__ __forceinline__ double2 ldv(const double2 *a, unsigned long long) { return *a; }
+__device__ __forceinline__ void stv(float4 *a, const float4 v, unsigned long long pol) { st4_pol(a, v, pol); }
+__device__ __forceinline__ void stv(double2 *a, const double2 v, unsigned long long) { *a = v; }
+
 // r -= alpha Ap on one vector; the new r^2 go into acc (one FMA per cell)
 __device__ __forceinline__ void upd_vec(float4 &r, const float4 a, float alpha, float &acc) {
   r.x = fmaf(-alpha, a.x, r.x);
@@ -432,27 +438,84 @@ __device__ __forceinline__ void upd_vec(double2 &r, const double2 a, double alph
 template <typename T>
 __device__ __forceinline__ T upd_range(typename Vec16<T>::type *__restrict__ r4,
                                        const typename Vec16<T>::type *__restrict__ a4, unsigned int lo,
-                                       unsigned int hi, unsigned int t0, unsigned int stride, T alpha) {
+                                       unsigned int hi, unsigned int t0, unsigned int stride, T alpha,
+                                       unsigned long long pr, unsigned long long pa) {
   typedef typename Vec16<T>::type V;
   T acc = 0;
   for (unsigned int q = lo + t0; q < hi; q += 2 * stride) {
     const unsigned int q2 = q + stride;
     const bool two = q2 < hi;
-    V rv0 = r4[q];
-    const V av0 = a4[q];
+    V rv0 = ldv(r4 + q, pr);
+    const V av0 = ldv(a4 + q, pa);
     V rv1, av1;
     if (two) {
-      rv1 = r4[q2];
-      av1 = a4[q2];
+      rv1 = ldv(r4 + q2, pr);
+      av1 = ldv(a4 + q2, pa);
     }
     upd_vec(rv0, av0, alpha, acc);
-    r4[q] = rv0;
+    stv(r4 + q, rv0, pr);
     if (two) {
       upd_vec(rv1, av1, alpha, acc);
-      r4[q2] = rv1;
+      stv(r4 + q2, rv1, pr);
     }
   }
   return acc;
+}
+
+// r -= alpha Ap in the reverse of the search kernel's plane order: the search
+// kernel gives each CTA a chunk of kz planes (nzc chunks) and all chunks
+// ascend together, so its last planes are the top ones of every chunk.  Here
+// virtual plane v = j * nzc + c is plane c kz + kz - 1 - j: the update starts
+// on the planes still in L2 and ends on the bottom ones, where the next
+// search kernel starts.  Plane vectors pv = 2^pv_shift.  Returns the sums of
+// r^2 over interior planes and over the two z-wall planes (non-periodic z).
+template <typename T>
+__device__ __forceinline__ void upd_range_rev(typename Vec16<T>::type *__restrict__ r4,
+                                              const typename Vec16<T>::type *__restrict__ a4, const GeoL &G,
+                                              int kz, int nzc, unsigned long long mnzc, int pv_shift,
+                                              unsigned int t0, unsigned int stride, T alpha, T &rr, T &wall,
+                                              unsigned long long pr, unsigned long long pa) {
+  typedef typename Vec16<T>::type V;
+  const unsigned int pmask = (1u << pv_shift) - 1u;
+  const unsigned int total = ((unsigned int)kz * (unsigned int)nzc) << pv_shift;
+  const bool zw = !G.pz;
+  // physical vector of virtual vector q (or ~0u past the last plane)
+  auto phys = [&](unsigned int q, bool &w) {
+    const unsigned int v = q >> pv_shift;
+    const unsigned int j = fdiv(v, mnzc);
+    const unsigned int c = v - j * (unsigned int)nzc;
+    const unsigned int z = c * (unsigned int)kz + (unsigned int)kz - 1u - j;
+    w = zw && (z == 0u || z == (unsigned int)G.nz - 1u);
+    return z < (unsigned int)G.nz ? (z << pv_shift) | (q & pmask) : ~0u;
+  };
+  for (unsigned int q = t0; q < total; q += 2 * stride) {
+    bool w0, w1 = false;
+    const unsigned int p0 = phys(q, w0);
+    const unsigned int p1 = q + stride < total ? phys(q + stride, w1) : ~0u;
+    V rv0, av0, rv1, av1;
+    if (p0 != ~0u) {
+      rv0 = ldv(r4 + p0, pr);
+      av0 = ldv(a4 + p0, pa);
+    }
+    if (p1 != ~0u) {
+      rv1 = ldv(r4 + p1, pr);
+      av1 = ldv(a4 + p1, pa);
+    }
+    if (p0 != ~0u) {
+      T a = 0;
+      upd_vec(rv0, av0, alpha, a);
+      stv(r4 + p0, rv0, pr);
+      if (w0) wall += a;
+      else rr += a;
+    }
+    if (p1 != ~0u) {
+      T a = 0;
+      upd_vec(rv1, av1, alpha, a);
+      stv(r4 + p1, rv1, pr);
+      if (w1) wall += a;
+      else rr += a;
+    }
+  }
 }
 
 // K2: r -= alpha Ap with (r,z) and (r,r); x += alpha p is left to the next
@@ -462,7 +525,8 @@ __device__ __forceinline__ T upd_range(typename Vec16<T>::type *__restrict__ r4,
 // two z-wall planes run in loops of their own with one weight each.
 template <typename T>
 __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r, const T *__restrict__ Ap,
-                                                 DevState *st, double *partials, int cond) {
+                                                 DevState *st, double *partials, int cond, int kz, int nzc,
+                                                 unsigned long long mnzc, int pv_shift, int l2hint) {
   __shared__ T s_dL[27], s_inv[27];
   __shared__ double s_red[2 * FNT / 32];
   pdl_sync();
@@ -479,20 +543,30 @@ __global__ void __launch_bounds__(FNT) k2_update(const GeoL G, T *__restrict__ r
   const unsigned int t0 = blockIdx.x * FNT + threadIdx.x;
   const unsigned int plane = (unsigned int)G.nx * (unsigned int)G.ny;
   if (G.px && G.py && (plane % E) == 0) {
+    // Ap is streamed (evict_first); r keeps the normal priority
+    const unsigned long long pr = l2_policy(0), pa = l2_policy(l2hint ? 1 : 0);
     V *r4 = reinterpret_cast<V *>(r);
     const V *a4 = reinterpret_cast<const V *>(Ap);
     const unsigned int pv = plane / E, nv = n / E;
     // vectors [wall_lo, wall_hi) of the interior planes, then the wall planes
     const unsigned int wall_lo = G.pz ? 0u : pv;
     const unsigned int wall_hi = G.pz ? nv : nv - pv;
-    rr = upd_range<T>(r4, a4, wall_lo, wall_hi, t0, stride, alpha);
+    if (kz > 0) {  // in the reverse of the search kernel's plane order
+      T in = 0, wl = 0;
+      upd_range_rev<T>(r4, a4, G, kz, nzc, mnzc, pv_shift, t0, stride, alpha, in, wl, pr, pa);
+      const int wc = 9 * (G.nz == 1 ? 2 : 1);
+      rr = in + wl;
+      if (!G.pz) corr = (s_inv[wc] - T(1)) * wl;
+    } else {
+    rr = upd_range<T>(r4, a4, wall_lo, wall_hi, t0, stride, alpha, pr, pa);
     if (!G.pz) {
       const int wc = 9 * (G.nz == 1 ? 2 : 1);
       const T w = s_inv[wc] - T(1);
-      T t = upd_range<T>(r4, a4, 0, wall_lo, t0, stride, alpha);
-      if (G.nz > 1) t += upd_range<T>(r4, a4, wall_hi, nv, t0, stride, alpha);
+      T t = upd_range<T>(r4, a4, 0, wall_lo, t0, stride, alpha, pr, pa);
+      if (G.nz > 1) t += upd_range<T>(r4, a4, wall_hi, nv, t0, stride, alpha, pr, pa);
       rr += t;
       corr = w * t;
+    }
     }
   } else {
     // general walls: per-cell class

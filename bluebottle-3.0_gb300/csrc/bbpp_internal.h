@@ -50,6 +50,7 @@ struct NetWork;     // learned-guess workspace (bbpp_net.cu)
 
 struct bbpp_tma_state;
 void *bbpp_tensor_map_encoder();  // cuTensorMapEncodeTiled, or null
+bool bbpp_tma_chunks(const bbpp_ctx *ctx, int *kz, int *nzc);  // z chunking of the TMA search kernel
 
 struct bbpp_ctx {
   bbpp_grid grid{};
@@ -86,6 +87,8 @@ struct bbpp_ctx {
   NetWork *net = nullptr;
   bbpp_tma_state *tma = nullptr;  // launch shape and tensor maps of the TMA search kernel
   bool pdl = false;               // iteration kernels launch with a programmatic dependency
+  bool rev_update = true;         // the update kernel walks the search kernel's planes in reverse
+  bool l2hint = true;             // FP32 iteration: mask evict_last in L2, p / Ap / x evict_first
   int inject = 0;                 // test hook of bbpp_debug_wait (see DevState::inject)
   long long wait_ns = 0;          // bound of device-side waits (0: one second)
 };
@@ -142,5 +145,5 @@ int bbpp_residual_async(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, c
 
 // learned initial guess (bbpp_net.cu)
 int bbpp_net_guess(bbpp_ctx *ctx, void *net, const uint8_t *mask, const double *rhs, const double *prev, double *x,
-                   double *ms);
+                   int coarsen, double *ms);
 void bbpp_net_ctx_free(bbpp_ctx *ctx);

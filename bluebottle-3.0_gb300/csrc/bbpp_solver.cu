@@ -267,6 +267,15 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
     // dominate the launch latency it hides)
     const char *e = getenv("BBPP_PDL");
     ctx->pdl = e && e[0] == '1';
+    // the update kernel's reversed plane order (BBPP_REV_UPDATE=0: ascending)
+    const char *ru = getenv("BBPP_REV_UPDATE");
+    ctx->rev_update = !(ru && ru[0] == '0');
+    // L2 eviction priorities of the FP32 iteration (BBPP_L2HINT=0: none).
+    // Measured at 256^3: the mask kept (evict_last) and p, Ap, x streamed
+    // (evict_first) save 1.3%; keeping r as well, with or without a
+    // persisting-L2 set-aside, is slower
+    const char *lh = getenv("BBPP_L2HINT");
+    ctx->l2hint = !(lh && lh[0] == '0');
   }
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
@@ -358,6 +367,7 @@ extern "C" void bbpp_default_opts(bbpp_opts *o) {
   o->ir_drop = 1e-2;
   o->net = nullptr;
   o->prev = nullptr;
+  o->net_coarsen = 0;
 }
 
 extern "C" const char *bbpp_status_str(int s) {
@@ -429,7 +439,23 @@ template <typename T>
 static void launch_update(bbpp_ctx *ctx, T *r, const T *Ap, DevState *st, int cond) {
   // bytes/cell: read r, Ap, write r
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_UPDATE : KK_UPDATE_F32, 3.0 * sizeof(T));
-  bbpp_launch(ctx, k2_update<T>, dim3(ctx->egrid), dim3(FNT), 0, ctx->GL, r, Ap, st, ctx->partials, cond);
+  // walk the planes in the reverse of the search kernel's order (its z chunks
+  // from the top down), so that both kernels start on the planes the other
+  // one touched last, still in L2; needs a power-of-two count of vectors per plane
+  int kz = 0, nzc = 0, shift = 0;
+  const int prec = sizeof(T) == 8 ? 1 : 0;
+  if (!(sizeof(T) == 4 && bbpp_tma_chunks(ctx, &kz, &nzc))) {
+    kz = ctx->pkz[prec];
+    nzc = (int)ctx->pgrid[prec].z;
+  }
+  const long long pv = (long long)ctx->GL.nx * ctx->GL.ny / (16 / (int)sizeof(T));
+  while (shift < 31 && (1ll << shift) < pv) shift++;
+  // FP64: the update is bound by the FP64 pipe, and the index arithmetic of the
+  // reversed walk costs more than the L2 hits save (measured 282 -> 297 ms)
+  if (sizeof(T) == 8 || (1ll << shift) != pv || (long long)kz * nzc * pv >= (1ll << 32) || ctx->rev_update == 0)
+    kz = 0;
+  bbpp_launch(ctx, k2_update<T>, dim3(ctx->egrid), dim3(FNT), 0, ctx->GL, r, Ap, st, ctx->partials, cond, kz, nzc,
+              div_magic((unsigned)std::max(nzc, 1)), shift, (int)(sizeof(T) == 4 && ctx->l2hint));
   bbpp_rec_end(ctx);
 }
 
@@ -759,6 +785,7 @@ static int check_opts(const bbpp_opts *o) {
   if (!(o->ir_drop >= 0.0 && o->ir_drop < 1.0)) return BBPP_BAD_ARG;
   if (!(o->tol >= 0) || o->max_iter < 0 || o->replace_every < 1) return BBPP_BAD_ARG;
   if (o->guess == BBPP_GUESS_LEARNED && !o->net) return BBPP_BAD_ARG;
+  if (o->net_coarsen < 0 || o->net_coarsen > 2) return BBPP_BAD_ARG;
   return 0;
 }
 
@@ -815,7 +842,7 @@ extern "C" int bbpp_solve(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs,
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   bool zero_x = o->guess == BBPP_GUESS_ZERO;
   if (o->guess == BBPP_GUESS_LEARNED) {
-    rc = bbpp_net_guess(ctx, o->net, mask, rhs, o->prev, x, &rep->guess_ms);
+    rc = bbpp_net_guess(ctx, o->net, mask, rhs, o->prev, x, o->net_coarsen, &rep->guess_ms);
     if (rc) return rep->status = rc;
     zero_x = false;
   }

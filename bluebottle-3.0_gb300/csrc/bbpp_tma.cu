@@ -81,21 +81,22 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned int 
   }
 }
 
+// tensor copies with an L2 eviction policy (l2_policy)
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, unsigned long long *bar, int c0,
-                                            int c1, int c2) {
+                                            int c1, int c2, unsigned long long pol) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], "
-      "[%2];" ::"r"(smem_addr(dst)),
-      "l"(map), "r"(smem_addr(bar)), "r"(c0), "r"(c1), "r"(c2)
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, "
+      "{%3, %4, %5}], [%2], %6;" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(smem_addr(bar)), "r"(c0), "r"(c1), "r"(c2), "l"(pol)
       : "memory");
 }
 
 __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, unsigned long long *bar, int c0,
-                                            int c1, int c2, int c3) {
+                                            int c1, int c2, int c3, unsigned long long pol) {
   asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, "
-      "%6}], [%2];" ::"r"(smem_addr(dst)),
-      "l"(map), "r"(smem_addr(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, "
+      "{%3, %4, %5, %6}], [%2], %7;" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(smem_addr(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "l"(pol)
       : "memory");
 }
 
@@ -108,9 +109,9 @@ struct TmaMaps {
 // Load rows [y, y + nrow) of plane z of one array into dst (row-major, nx
 // floats per row).  4-D maps split x into 256-wide pieces (nx > 256).
 __device__ __forceinline__ void load_rows(float *dst, const CUtensorMap *map, unsigned long long *bar, int y, int z,
-                                          bool four_d) {
-  if (four_d) tma_load_4d(dst, map, bar, 0, 0, y, z);
-  else tma_load_3d(dst, map, bar, 0, y, z);
+                                          bool four_d, unsigned long long pol) {
+  if (four_d) tma_load_4d(dst, map, bar, 0, 0, y, z, pol);
+  else tma_load_3d(dst, map, bar, 0, y, z, pol);
 }
 
 }  // namespace
@@ -120,7 +121,8 @@ template <int NPT, bool MASK, bool ISO>
 __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constant__ TmaMaps M,
                                               float *__restrict__ pnew, float *__restrict__ Ap,
                                               float *__restrict__ x, const uint8_t *__restrict__ mask,
-                                              DevState *st, double *partials, int ty, int kz, int ns, int four_d) {
+                                              DevState *st, double *partials, int ty, int kz, int ns, int four_d,
+                                              int l2hint) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   __shared__ float s_dL[27], s_inv[27];
   __shared__ double s_red[TNT / 32];
@@ -137,6 +139,10 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   // for them runs out and the solve ends with DONE_TIMEOUT
   const bool skip_one = *(volatile int *)&st->inject && blockIdx.x == 0 && blockIdx.y == 0;
   load_tabs<float>(G, s_dL, s_inv);
+  // L2 policies: the mask, read by every search kernel, stays (evict_last);
+  // p, Ap and x stream through (evict_first); r keeps the normal priority
+  const unsigned long long pol_r = l2_policy(0), pol_stream = l2_policy(l2hint ? 1 : 0);
+  const unsigned long long pol_mask = l2_policy(l2hint ? 2 : 0);
 
   const int tid = threadIdx.x, lane = tid & 31;
   const int nx = G.nx, ny = G.ny, nz = G.nz;
@@ -166,14 +172,14 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
     float *rs = stage + (size_t)s * 2 * arr;
     unsigned long long *bar = &s_full[s];
     mbar_expect_tx(bar, tx_bytes);
-    load_rows(rs + nx, &M.r_rows, bar, y0, zr, four_d);
-    load_rows(rs, &M.r_row, bar, ys, zr, four_d);
-    load_rows(rs + (ty + 1) * nx, &M.r_row, bar, yn, zr, four_d);
+    load_rows(rs + nx, &M.r_rows, bar, y0, zr, four_d, pol_r);
+    load_rows(rs, &M.r_row, bar, ys, zr, four_d, pol_r);
+    load_rows(rs + (ty + 1) * nx, &M.r_row, bar, yn, zr, four_d, pol_r);
     if (!first) {
       float *ps = rs + arr;
-      load_rows(ps + nx, &M.p_rows, bar, y0, zr, four_d);
-      load_rows(ps, &M.p_row, bar, ys, zr, four_d);
-      load_rows(ps + (ty + 1) * nx, &M.p_row, bar, yn, zr, four_d);
+      load_rows(ps + nx, &M.p_rows, bar, y0, zr, four_d, pol_stream);
+      load_rows(ps, &M.p_row, bar, ys, zr, four_d, pol_stream);
+      load_rows(ps + (ty + 1) * nx, &M.p_row, bar, yn, zr, four_d, pol_stream);
     }
   };
 
@@ -238,8 +244,11 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
     for (int k = 0; k < NPT; k++) {
       const int row = orow[k], c4 = oc4[k];
       const unsigned int c = plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + row) + 4u * c4;
-      if (MASK) mk[k] = *reinterpret_cast<const uchar4 *>(mask + c);
-      if (lag) xv[k] = *reinterpret_cast<const float4 *>(x + c);
+      if (MASK) {
+        const unsigned int m = ld_u32_pol(mask + c, pol_mask);
+        mk[k] = make_uchar4(m & 0xffu, (m >> 8) & 0xffu, (m >> 16) & 0xffu, m >> 24);
+      }
+      if (lag) xv[k] = ld4_pol(reinterpret_cast<const float4 *>(x + c), pol_stream);
     }
   };
 
@@ -297,8 +306,8 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
       acc = fmaf(c.z, a2, acc);
       acc = fmaf(c.w, a3, acc);
       const unsigned int g = plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + row) + 4u * c4;
-      *reinterpret_cast<float4 *>(Ap + g) = make_float4(a0, a1, a2, a3);
-      *reinterpret_cast<float4 *>(pnew + g) = c;
+      st4_pol(reinterpret_cast<float4 *>(Ap + g), make_float4(a0, a1, a2, a3), pol_stream);
+      st4_pol(reinterpret_cast<float4 *>(pnew + g), c, pol_stream);
       if (lag) {
         const float4 q = *reinterpret_cast<const float4 *>(po + off);
         float4 xo = xv[k];
@@ -306,7 +315,7 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
         xo.y = fmaf(alpha, q.y, xo.y);
         xo.z = fmaf(alpha, q.z, xo.z);
         xo.w = fmaf(alpha, q.w, xo.w);
-        *reinterpret_cast<float4 *>(x + g) = xo;
+        st4_pol(reinterpret_cast<float4 *>(x + g), xo, pol_stream);
       }
     }
   };
@@ -499,6 +508,14 @@ void bbpp_tma_free(bbpp_ctx *ctx) {
   ctx->tma = nullptr;
 }
 
+// z chunking of the TMA search kernel: kz planes per CTA, nzc chunks
+bool bbpp_tma_chunks(const bbpp_ctx *ctx, int *kz, int *nzc) {
+  if (!ctx->tma || !ctx->tma->ok) return false;
+  *kz = ctx->tma->kz;
+  *nzc = (int)ctx->tma->grid.y;
+  return true;
+}
+
 size_t bbpp_tma_partials(const bbpp_ctx *ctx) {
   return (ctx->tma && ctx->tma->ok) ? (size_t)ctx->tma->grid.x * ctx->tma->grid.y : 0;
 }
@@ -532,7 +549,7 @@ bool bbpp_tma_search(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const f
   M.p_row = mp.row;
 #define BBPP_TMA_LAUNCH(N, MK, IS)                                                                          \
   bbpp_launch(ctx, k1_tma<N, MK, IS>, t->grid, dim3(TNT), (size_t)t->smem, ctx->GL, M, pnew, Ap, x, mask, st, \
-              ctx->partials, t->ty, t->kz, t->ns, t->four_d)
+              ctx->partials, t->ty, t->kz, t->ns, t->four_d, (int)ctx->l2hint)
 #define BBPP_TMA_NPT(N)                            \
   if (mask) {                                      \
     if (ctx->GL.iso) BBPP_TMA_LAUNCH(N, true, true);   \

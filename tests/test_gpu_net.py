@@ -189,6 +189,71 @@ def test_net_checkpoint_roundtrip(bbpp_lib, tmp_path):
     assert np.array_equal(other.get_params(), p)
 
 
+def _restrict2(a):
+    nz, ny, nx = a.shape
+    return a.reshape(nz // 2, 2, ny // 2, 2, nx // 2, 2).mean(axis=(1, 3, 5))
+
+
+def _prolong2(c, periodic):
+    """Cell-centred trilinear interpolation by 2 (weights 3/4, 1/4 per axis);
+    periodic axes wrap, the others repeat the edge cell.  Axes [z, y, x]."""
+    out = c
+    for ax in range(3):
+        n = out.shape[ax]
+        fi = (np.arange(2 * n) + 0.5) / 2 - 0.5
+        lo = np.floor(fi).astype(int)
+        w = fi - lo
+        if periodic[ax]:
+            lo_c, hi_c = lo % n, (lo + 1) % n
+        else:
+            lo_c, hi_c = np.clip(lo, 0, n - 1), np.clip(lo + 1, 0, n - 1)
+        sh = [1, 1, 1]
+        sh[ax] = -1
+        out = np.take(out, lo_c, axis=ax) * (1 - w).reshape(sh) + np.take(out, hi_c, axis=ax) * w.reshape(sh)
+    return out
+
+
+@pytest.mark.parametrize("bc", ["ppn", "nnn"])
+def test_coarse_guess_matches_restatement(bbpp_lib, bc):
+    """The learned guess on the grid restricted by 2: the solver's guess equals
+    p_prev + prolong2(net(restrict2(r, p_prev, mask)) - restrict2(p_prev)), with
+    the network run directly on numpy-restricted inputs, coarse solid cells
+    (>= 4 solid children) carrying no correction and fine solid cells 0."""
+    nx, ny, nz = 32, 16, 24
+    g = problems.make_grid(nx, bc, ny=ny, nz=nz)
+    rng = np.random.default_rng(5)
+    mask = np.zeros((nz, ny, nx), np.uint8)
+    mask[6:11, 3:8, 10:17] = 1
+    mask[15:17, 9:12, 2:4] = 1
+    rhs = rng.normal(size=(nz, ny, nx))
+    rhs[mask == 1] = 0
+    prev = rng.normal(size=(nz, ny, nx))
+    s = bbpp.Solver(g)
+    dmask, drhs, dprev = (bbpp.DeviceArray.from_host(a) for a in (mask, rhs, prev))
+    net = learned.Net(seed=4)
+    dx = bbpp.DeviceArray((nz, ny, nx), np.float64)
+    rep = s.solve(drhs, dx, dmask, tol=1e300, precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle,
+                  prev=dprev.ptr, net_coarsen=2)
+    assert rep.iters == 0
+    got = dx.download()
+    # the same on the host: residual of the warm start (solver's kernel), restriction, network, prolongation
+    dr = bbpp.DeviceArray((nz, ny, nx), np.float64)
+    s.residual(drhs, dprev, dr, dmask)
+    r = dr.download()
+    rc, pc = _restrict2(r), _restrict2(prev)
+    mc = (_restrict2(mask.astype(np.float64)) >= 0.5).astype(np.uint8)
+    d_rc, d_pc, d_mc = (bbpp.DeviceArray.from_host(a) for a in (rc, pc, mc))
+    d_o = bbpp.DeviceArray(rc.shape, np.float64)
+    net.infer((nx // 2, ny // 2, nz // 2), 4 * g.dx * g.dy, d_rc, d_pc, d_mc, d_o)
+    corr = np.where(mc == 1, 0.0, d_o.download() - pc)
+    periodic = [bc[2] == "p", bc[1] == "p", bc[0] == "p"]
+    want = np.where(mask == 1, 0.0, prev + _prolong2(corr, periodic))
+    scale = np.abs(want - prev).max()
+    assert scale > 0
+    assert np.abs(got - want).max() <= 1e-3 * scale
+    net.close()
+
+
 def test_learned_guess_gain(bbpp_lib):
     """Train on an OU sequence at 32^3 and compare PCG iterations on held-out
     steps: zero guess (the reference), warm start from p_prev, learned."""
