@@ -237,9 +237,11 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
     oc4[k] = e - orow[k] * nxv;
   }
   // own-cell mask and x of the next plane, loaded one plane ahead
-  uchar4 mk[NPT];
-  float4 xv[NPT];
-  auto fetch = [&](int zc) {
+  // two register sets, alternating by plane: the loads of plane j + 2 are in
+  // flight while plane j is computed
+  uchar4 mkA[NPT], mkB[NPT];
+  float4 xvA[NPT], xvB[NPT];
+  auto fetch = [&](int zc, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
 #pragma unroll
     for (int k = 0; k < NPT; k++) {
       const int row = orow[k], c4 = oc4[k];
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   };
 
   float acc = 0.f;
-  auto stencil = [&](int j) {
+  auto stencil = [&](int j, const uchar4 (&mk)[NPT], const float4 (&xv)[NPT]) {
     const int zc = z0 - 1 + j;
     const float *cs = stage + (size_t)(j % ns) * 2 * arr;           // p_new, plane z
     const float *ts = stage + (size_t)((j + 1) % ns) * 2 * arr;     // plane z+1
@@ -324,17 +326,23 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
     const int pre = min(ns, np);
     for (int j = 0; j < pre; j++) issue(j);
   }
-  fetch(z0);
+  const int nj = z1 - z0;  // planes of this CTA: j = 1 .. nj
+  fetch(z0, mkA, xvA);
+  if (nj >= 2) fetch(z0 + 1, mkB, xvB);
   prep(0);
   prep(1);
-  for (int j = 1; j <= z1 - z0; j++) {
+  auto step = [&](int j, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
     prep(j + 1);
     fence_proxy_async();  // this thread's stage writes before later tensor copies
     __syncthreads();
     if (tid == 0 && j >= 2 && j - 2 + ns < np) issue(j - 2 + ns);
-    // the mask / x registers of plane j are consumed here, then refilled
-    stencil(j);
-    if (j < z1 - z0) fetch(z0 + j);
+    // the mask / x registers of plane j are consumed here, then refilled with plane j + 2
+    stencil(j, mk, xv);
+    if (j + 2 <= nj) fetch(z0 + j + 1, mk, xv);
+  };
+  for (int j = 1; j <= nj; j += 2) {
+    step(j, mkA, xvA);
+    if (j + 1 <= nj) step(j + 1, mkB, xvB);
   }
 
   if (__syncthreads_or(bad)) {
