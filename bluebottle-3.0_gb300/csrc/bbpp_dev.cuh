@@ -62,6 +62,7 @@ struct DevState {
   int rep_now;
   int inject;            // test hook: 1 = the first TMA search CTA skips the copies of one plane
   long long wait_ns;     // bound of a device-side wait (0: one second)
+  int fq;                // fused iteration kernels completed in this solve
 };
 
 // Set by the last CTA of a search kernel: does this iteration's checkpoint
@@ -224,6 +225,24 @@ __device__ __forceinline__ void finish_iteration(DevState *st, double rz1, doubl
     st->rz = rz1;
     if (it > st->max_iter) st->done = DONE_MAX_ITER;
   }
+}
+
+// End of an iteration whose update a fused kernel deferred: its residual's
+// products rz1, rr1 are known; the next beta comes from the fused kernel's
+// expansion, so only rz is kept (the base of that expansion).
+__device__ __forceinline__ void finish_deferred(DevState *st, double rz1, double rr1) {
+  const int it = st->iter + 1;
+  st->iter = it;
+  st->rz_last = rz1;
+  st->rr = rr1;
+  const bool conv = (st->stop == 0) ? (rz1 <= st->tol2bb) : (rr1 <= st->tol2bb);
+  if (isnan(rz1)) {
+    st->done = DONE_NAN;
+    return;
+  }
+  st->rz = rz1;
+  if (conv) st->done = (it > st->max_iter) ? DONE_MAX_ITER : ((st->stop == 0) ? DONE_CONVERGED : DONE_PENDING);
+  else if (it > st->max_iter) st->done = DONE_MAX_ITER;
 }
 
 }  // namespace bbpp

@@ -705,6 +705,7 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       st->rz_last = rz1;
       st->rr = rr1;
       st->iter = 0;
+      st->fq = 0;
       st->first = 1;
       st->dlag = 0;
       st->replacements = 0;

@@ -18,11 +18,13 @@ struct GraphKey {
   bool rr = false;
   double bscale = 1.0;
   const void *xhi = nullptr, *rhs64 = nullptr;
+  const void *r1 = nullptr, *Ap1 = nullptr;  // fused iterations: the second r and Ap buffers
   cudaStream_t stream = nullptr;
   bool operator==(const GraphKey &o) const {
     return mask == o.mask && rhs == o.rhs && x == o.x && r == o.r && p0 == o.p0 && p1 == o.p1 && Ap == o.Ap &&
            st == o.st && len == o.len && replace_every == o.replace_every && elem == o.elem && rr == o.rr &&
-           bscale == o.bscale && xhi == o.xhi && rhs64 == o.rhs64 && stream == o.stream;
+           bscale == o.bscale && xhi == o.xhi && rhs64 == o.rhs64 && r1 == o.r1 && Ap1 == o.Ap1 &&
+           stream == o.stream;
   }
 };
 
@@ -36,7 +38,7 @@ struct KEv {
 };
 
 enum KernelKind { KK_SEARCH_SPMV = 0, KK_UPDATE, KK_AXPY, KK_RESID, KK_SEARCH_SPMV_F32, KK_UPDATE_F32,
-                  KK_AXPY_F32, KK_RESID_F32, KK_COUNT };
+                  KK_AXPY_F32, KK_RESID_F32, KK_FUSED_F32, KK_COUNT };
 
 struct GraphCache {
   GraphKey key;
@@ -89,6 +91,7 @@ struct bbpp_ctx {
   bool pdl = false;               // iteration kernels launch with a programmatic dependency
   bool rev_update = true;         // the update kernel walks the search kernel's planes in reverse
   bool l2hint = true;             // FP32 iteration: mask evict_last in L2, p / Ap / x evict_first
+  bool fused = true;              // FP32 reliable-update solves: one fused kernel per iteration
   int inject = 0;                 // test hook of bbpp_debug_wait (see DevState::inject)
   long long wait_ns = 0;          // bound of device-side waits (0: one second)
 };
@@ -139,6 +142,15 @@ void bbpp_set_reliable(double *xhi, const double *rhs);
 void bbpp_tma_init(bbpp_ctx *ctx);
 void bbpp_tma_free(bbpp_ctx *ctx);
 size_t bbpp_tma_partials(const bbpp_ctx *ctx);
+bool bbpp_tma_fused_ok(const bbpp_ctx *ctx);
+bool bbpp_tma_fused_maps(bbpp_ctx *ctx, const float *const r[2], const float *const a[2], const float *const p[2]);
+// FP32 PCG loop with one fused kernel per iteration (bbpp_solver.cu)
+int bbpp_pcg_loop_fused(bbpp_ctx *ctx, const uint8_t *mask, const float *rhs, float *x, float *const r[2],
+                        float *const p[2], float *const Ap[2], bbpp::DevState *st, bbpp::DevState *hst,
+                        int replace_every, bool confirm, int *iters_out);
+// the fused FP32 iteration kernel (update of the pending step + search step)
+bool bbpp_tma_fused(bbpp_ctx *ctx, const uint8_t *mask, const float *rin, const float *apin, const float *pold,
+                    float *rout, float *pnew, float *apout, float *x, bbpp::DevState *st);
 bool bbpp_tma_search(bbpp_ctx *ctx, const uint8_t *mask, const float *r, const float *pold, float *pnew, float *Ap,
                      float *x, bbpp::DevState *st);
 int bbpp_residual_async(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const double *x, double *r);

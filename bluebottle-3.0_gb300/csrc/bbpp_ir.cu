@@ -29,6 +29,7 @@ using namespace bbpp;
 
 struct IrBuffers {
   float *r = nullptr, *d = nullptr, *rd = nullptr, *p[2] = {nullptr, nullptr}, *Ap = nullptr;
+  float *rd2 = nullptr, *Ap2 = nullptr;  // second residual and Ap buffers of the fused iterations
 };
 
 void bbpp_ir_free(bbpp_ctx *ctx) {
@@ -40,6 +41,8 @@ void bbpp_ir_free(bbpp_ctx *ctx) {
   cudaFree(b->p[0]);
   cudaFree(b->p[1]);
   cudaFree(b->Ap);
+  cudaFree(b->rd2);
+  cudaFree(b->Ap2);
   delete b;
   ctx->ir = nullptr;
 }
@@ -84,8 +87,19 @@ static int solve_reliable(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs,
   bbpp_set_reliable(x, rhs);
   float *const p[2] = {b->p[0], b->p[1]};
   int it = 0;
-  rc = bbpp_pcg_loop<float>(ctx, mask, b->r, b->d, b->rd, p, b->Ap, st, hst, o->replace_every,
-                            o->stop == BBPP_STOP_TRUE_REL, true, &it);
+  bool fused = ctx->fused && bbpp_tma_fused_ok(ctx);
+  if (fused && !b->rd2) {
+    CK(cudaMalloc(&b->rd2, sizeof(float) * n));
+    CK(cudaMalloc(&b->Ap2, sizeof(float) * n));
+  }
+  float *const rs[2] = {b->rd, b->rd2}, *const as[2] = {b->Ap, b->Ap2};
+  if (fused) fused = bbpp_tma_fused_maps(ctx, rs, as, p);
+  if (fused)
+    rc = bbpp_pcg_loop_fused(ctx, mask, b->r, b->d, rs, p, as, st, hst, o->replace_every,
+                             o->stop == BBPP_STOP_TRUE_REL, &it);
+  else
+    rc = bbpp_pcg_loop<float>(ctx, mask, b->r, b->d, b->rd, p, b->Ap, st, hst, o->replace_every,
+                              o->stop == BBPP_STOP_TRUE_REL, true, &it);
   bbpp_set_reliable(nullptr, nullptr);
   if (rc) return rc;  // the loop's last fold has brought x up to date
   rep->iters = it;

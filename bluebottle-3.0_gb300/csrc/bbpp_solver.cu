@@ -276,6 +276,9 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
     // persisting-L2 set-aside, is slower
     const char *lh = getenv("BBPP_L2HINT");
     ctx->l2hint = !(lh && lh[0] == '0');
+    // one fused kernel per FP32 iteration (BBPP_FUSED=0: search and update kernels)
+    const char *fu = getenv("BBPP_FUSED");
+    ctx->fused = !(fu && fu[0] == '0');
   }
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
@@ -582,26 +585,9 @@ static void launch_iteration(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T
 
 // Capture (or reuse) the graph of iterations q0+1 .. q0+len for these buffers.
 // Returns its index in ctx->graphs, or -1 after a CUDA error.
-template <typename T>
-static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
-                           DevState *st, int len, int replace_every, bool rr, cudaGraphExec_t *out) {
-  GraphKey key;
-  key.mask = mask;
-  key.rhs = rhs;
-  key.x = x;
-  key.r = r;
-  key.p0 = p[0];
-  key.p1 = p[1];
-  key.Ap = Ap;
-  key.st = st;
-  key.len = len;
-  key.replace_every = replace_every;
-  key.rr = rr;
-  key.elem = (int)sizeof(T);
-  key.stream = ctx->stream;
-  key.bscale = t_bscale;
-  key.xhi = t_rel.xhi;
-  key.rhs64 = t_rel.rhs;
+// Capture len iterations (launch(i), i = 1 .. len) into a cached graph.
+template <typename F>
+static int capture_chunk(bbpp_ctx *ctx, const GraphKey &key, int len, F launch, cudaGraphExec_t *out) {
   for (auto &gc : ctx->graphs)
     if (gc.key == key) {
       *out = gc.exec;
@@ -619,7 +605,7 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   ctx->rec = nullptr;  // graphs carry no profiling events
   for (int i = 1; i <= len; i++) {
     ctx->rec_iter = i;
-    launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, i, replace_every, rr);
+    launch(i);
   }
   ctx->rec = nullptr;
   e = cudaStreamEndCapture(ctx->stream, &graph);
@@ -645,7 +631,31 @@ static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *
   gc.kernels = (int)(nnodes - 2 * gc.evs.size());
   ctx->graphs.push_back(gc);
   *out = exec;
-  return (int)ctx->graphs.size() - 1 + 0 * BBPP_CONVERGED;
+  return (int)ctx->graphs.size() - 1;
+}
+
+template <typename T>
+static int get_chunk_graph(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, T *const p[2], T *Ap,
+                           DevState *st, int len, int replace_every, bool rr, cudaGraphExec_t *out) {
+  GraphKey key;
+  key.mask = mask;
+  key.rhs = rhs;
+  key.x = x;
+  key.r = r;
+  key.p0 = p[0];
+  key.p1 = p[1];
+  key.Ap = Ap;
+  key.st = st;
+  key.len = len;
+  key.replace_every = replace_every;
+  key.rr = rr;
+  key.elem = (int)sizeof(T);
+  key.stream = ctx->stream;
+  key.bscale = t_bscale;
+  key.xhi = t_rel.xhi;
+  key.rhs64 = t_rel.rhs;
+  return capture_chunk(
+      ctx, key, len, [&](int i) { launch_iteration<T>(ctx, mask, rhs, x, r, p, Ap, st, i, replace_every, rr); }, out);
 }
 
 static int status_of(int done) {
@@ -737,6 +747,113 @@ int bbpp_pcg_loop(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
   ctx->launches += 1;
   CK(cudaGetLastError());
   if (iters_out) *iters_out = q;
+  return 0;
+}
+
+// ---------------------------------------------------- fused iterations --
+// Iteration q (1-based) is one kernel: it reads r[(q-1)&1], Ap[(q-1)&1] and
+// p[(q-1)&1], writes r[q&1], Ap[q&1] and p[q&1], and leaves its own step
+// (alpha_q p_q into x, alpha_q Ap_q out of r) pending for the next kernel or
+// for the fold and residual kernels of a replacement or confirmation, which
+// write r[q&1].  The host counts kernels (st->fq); an iteration ends (st->iter)
+// in the kernel after it.
+static void launch_fused(bbpp_ctx *ctx, const uint8_t *mask, const float *rhs, float *x, float *const r[2],
+                         float *const p[2], float *const Ap[2], DevState *st, int q, int replace_every) {
+  const int i = (q - 1) & 1, o = q & 1;
+  // bytes/cell: read r, Ap, p_old, x (+ mask), write r, p, Ap, x
+  bbpp_rec_begin(ctx, KK_FUSED_F32, 32.0 + (mask ? 1 : 0));
+  bbpp_tma_fused(ctx, mask, r[i], Ap[i], p[i], r[o], p[o], Ap[o], x, st);
+  bbpp_rec_end(ctx);
+  // checkpoint: the kernel has decided between the recursive residual and a
+  // replacement; the replacement kernels return at once without one
+  if (q % replace_every == 0) launch_replace<float>(ctx, mask, x, rhs, r[o], p[o], st, RES_ITER);
+}
+
+int bbpp_pcg_loop_fused(bbpp_ctx *ctx, const uint8_t *mask, const float *rhs, float *x, float *const r[2],
+                        float *const p[2], float *const Ap[2], DevState *st, DevState *hst, int replace_every,
+                        bool confirm, int *iters_out) {
+  const int chunk = (replace_every % 2 == 0) ? replace_every : 2 * replace_every;
+  CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int q = hst->fq;
+  long long rounds = 0;
+  const long long max_rounds = 4ll * (hst->max_iter / 1 + 2) + 64;
+  auto per_launch = [&](int qq) { return (qq % replace_every == 0) ? 3 : 1; };
+  while (hst->done == RUNNING) {
+    if (++rounds > max_rounds) {
+      bbpp_record_error(ctx, cudaErrorUnknown, "solve loop made no progress", __LINE__);
+      return BBPP_CUDA_ERROR;
+    }
+    const int q0 = q;
+    int gi = -1;
+    std::vector<KEv> single;
+    if (q % chunk == 0 && !ctx->profiling) {
+      GraphKey key;
+      key.mask = mask;
+      key.rhs = rhs;
+      key.x = x;
+      key.r = r[0];
+      key.r1 = r[1];
+      key.p0 = p[0];
+      key.p1 = p[1];
+      key.Ap = Ap[0];
+      key.Ap1 = Ap[1];
+      key.st = st;
+      key.len = chunk;
+      key.replace_every = replace_every;
+      key.elem = 4;
+      key.stream = ctx->stream;
+      key.bscale = t_bscale;
+      key.xhi = t_rel.xhi;
+      key.rhs64 = t_rel.rhs;
+      cudaGraphExec_t exec;
+      gi = capture_chunk(
+          ctx, key, chunk, [&](int i) { launch_fused(ctx, mask, rhs, x, r, p, Ap, st, i, replace_every); }, &exec);
+      if (gi < 0) return BBPP_CUDA_ERROR;
+      CK(cudaGraphLaunch(exec, ctx->stream));
+      ctx->launches += ctx->graphs[gi].kernels;
+    } else if (q % chunk == 0) {
+      ctx->rec = &single;
+      for (int i = 1; i <= chunk; i++) {
+        ctx->rec_iter = i;
+        launch_fused(ctx, mask, rhs, x, r, p, Ap, st, q + i, replace_every);
+        ctx->launches += per_launch(q + i);
+      }
+      ctx->rec = nullptr;
+      CK(cudaGetLastError());
+    } else {
+      if (ctx->profiling) ctx->rec = &single;
+      ctx->rec_iter = 1;
+      launch_fused(ctx, mask, rhs, x, r, p, Ap, st, q + 1, replace_every);
+      ctx->rec = nullptr;
+      ctx->launches += per_launch(q + 1);
+      CK(cudaGetLastError());
+    }
+    CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    q = hst->fq;
+    if (ctx->profiling) {
+      if (gi >= 0) bbpp_rec_collect(ctx, ctx->graphs[gi].evs, q - q0, false);
+      else bbpp_rec_collect(ctx, single, q - q0, true);
+    }
+    if (hst->done == DONE_PENDING) {
+      if (!confirm) {
+        hst->done = DONE_CONVERGED;
+        CK(cudaMemcpyAsync(&st->done, &hst->done, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        break;
+      }
+      launch_replace<float>(ctx, mask, x, rhs, r[q & 1], p[q & 1], st, RES_CONFIRM);
+      ctx->launches += 2;
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(hst, st, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  // x still lacks the pending step unless a replacement or confirmation came last
+  k_fold<<<ctx->egrid, FNT, 0, ctx->stream>>>(ctx->GL, t_rel.xhi, x, p[q & 1], st, 0);
+  ctx->launches += 1;
+  CK(cudaGetLastError());
+  if (iters_out) *iters_out = hst->iter;
   return 0;
 }
 
@@ -1104,8 +1221,8 @@ extern "C" int bbpp_flush_l2(void) {
 }
 
 // ----------------------------------------------------------- kernel stats --
-static const char *kk_name[KK_COUNT] = {"search_spmv", "update", "axpy_x", "resid",
-                                        "search_spmv_f32", "update_f32", "axpy_x_f32", "resid_f32"};
+static const char *kk_name[KK_COUNT] = {"search_spmv", "update", "axpy_x", "resid", "search_spmv_f32",
+                                        "update_f32", "axpy_x_f32", "resid_f32", "fused_f32"};
 
 void bbpp_rec_begin(bbpp_ctx *ctx, int kind, double bytes_per_cell) {
   if (!ctx->rec) return;

@@ -28,6 +28,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 
@@ -365,6 +366,319 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   }
 }
 
+// ------------------------------------------------------- fused iteration --
+// One kernel per PCG iteration (FP32).  Iteration q's search kernel also does
+// the update of iteration q - 1, which the two-kernel form leaves to a kernel
+// of its own: on every staged row (the halo rows too)
+//   r_{q-1} = r_{q-2} - alpha_{q-1} Ap_{q-1}      (when a step is pending)
+//   p_q = z_{q-1} + beta_q p_{q-1},   z = r / dL on wall classes
+// then, one plane behind, Ap_q = L p_q on the slab's own cells, the stores of
+// r_{q-1}, p_q, Ap_q, x += alpha_{q-1} p_{q-1}, and five partial sums:
+// (p_q, Ap_q), (r,z) and (r,r) of r_{q-1}, (Ap_q, z_{q-1}), (Ap_q, Ap_q / dL).
+// beta_q cannot wait for (r_{q-1}, z_{q-1}), so it comes from the expansion
+//   (r_{q-1}, z_{q-1}) = (r_{q-2}, z_{q-2}) - 2 alpha (Ap, z) + alpha^2 (Ap, Ap / dL)
+// evaluated in FP64 at the end of the previous kernel; the exact value, summed
+// here, restarts the expansion every iteration (alpha_q uses it), so no error
+// accumulates.  The exact (r,z), (r,r) of r_{q-1} end iteration q - 1 (the
+// convergence test runs one kernel late, on a settled x, r pair).  Traffic:
+// r, Ap, p_old, x, mask in (17 B/cell) and r, p, Ap, x out (16 B/cell), in one
+// kernel, against 37 B/cell in two.  r and Ap are double-buffered: a CTA's
+// halo rows are another CTA's own cells.
+struct FusedMaps {
+  CUtensorMap r_rows, r_row, a_rows, a_row, p_rows, p_row;
+};
+
+template <int NPT, bool MASK, bool ISO>
+__global__ void __launch_bounds__(TNT) k1_fused(const GeoL G, const __grid_constant__ FusedMaps M,
+                                                float *__restrict__ rout, float *__restrict__ pnew,
+                                                float *__restrict__ Apout, float *__restrict__ x,
+                                                const uint8_t *__restrict__ mask, DevState *st, double *partials,
+                                                int ty, int kz, int ns, int four_d, int l2hint) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ float s_dL[27], s_inv[27];
+  __shared__ double s_red[5 * TNT / 32];
+  __shared__ unsigned long long s_full[8];
+  pdl_sync();
+  if (*(volatile int *)&st->done) return;
+  const bool first = *(volatile int *)&st->first;
+  const float beta = first ? 0.f : (float)(*(volatile double *)&st->beta);
+  const bool lag = !first && *(volatile int *)&st->dlag;  // a step is pending: r and x take alpha of it
+  const float alpha = lag ? (float)(*(volatile double *)&st->alpha) : 0.f;
+  const long long wl = *(volatile long long *)&st->wait_ns;
+  const unsigned long long limit = wl > 0 ? (unsigned long long)wl : 1000000000ull;
+  const bool skip_one = *(volatile int *)&st->inject && blockIdx.x == 0 && blockIdx.y == 0;
+  load_tabs<float>(G, s_dL, s_inv);
+  const unsigned long long pol_n = l2_policy(0), pol_stream = l2_policy(l2hint ? 1 : 0);
+  const unsigned long long pol_mask = l2_policy(l2hint ? 2 : 0);
+
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const int nxv = nx >> 2;
+  const int rows = ty + 2;
+  const int arr = rows * nx;
+  float *stage = reinterpret_cast<float *>(smem_raw);  // [ns][3][rows][nx]: r, Ap_old -> p_new, p_old
+  const int y0 = blockIdx.x * ty;
+  const int z0 = blockIdx.y * kz, z1 = min(z0 + kz, nz);
+  const int np = z1 - z0 + 2;
+  const unsigned int plane = (unsigned int)nx * (unsigned int)ny;
+  const unsigned int tx_bytes = (unsigned int)((1 + (lag ? 1 : 0) + (first ? 0 : 1)) * arr * 4);
+  const int ys = G.py ? (y0 - 1 + ny) % ny : y0 - 1;
+  const int yn = G.py ? (y0 + ty) % ny : y0 + ty;
+
+  if (tid == 0) {
+    for (int s = 0; s < ns; s++) mbar_init(&s_full[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  auto issue = [&](int j) {
+    if (skip_one && j == 2) return;
+    const int s = j % ns;
+    int zr = z0 - 1 + j;
+    if (G.pz) zr = (zr + nz) % nz;
+    float *rs = stage + (size_t)s * 3 * arr;
+    unsigned long long *bar = &s_full[s];
+    mbar_expect_tx(bar, tx_bytes);
+    load_rows(rs + nx, &M.r_rows, bar, y0, zr, four_d, pol_n);
+    load_rows(rs, &M.r_row, bar, ys, zr, four_d, pol_n);
+    load_rows(rs + (ty + 1) * nx, &M.r_row, bar, yn, zr, four_d, pol_n);
+    if (lag) {
+      float *as = rs + arr;
+      load_rows(as + nx, &M.a_rows, bar, y0, zr, four_d, pol_n);
+      load_rows(as, &M.a_row, bar, ys, zr, four_d, pol_n);
+      load_rows(as + (ty + 1) * nx, &M.a_row, bar, yn, zr, four_d, pol_n);
+    }
+    if (!first) {
+      float *ps = rs + 2 * arr;
+      load_rows(ps + nx, &M.p_rows, bar, y0, zr, four_d, pol_stream);
+      load_rows(ps, &M.p_row, bar, ys, zr, four_d, pol_stream);
+      load_rows(ps + (ty + 1) * nx, &M.p_row, bar, yn, zr, four_d, pol_stream);
+    }
+  };
+
+  bool bad = false;
+  // over a stage: r -= alpha Ap_old in place, p_new into the Ap_old slot
+  auto prep = [&](int j) {
+    const int s = j % ns;
+    if (!mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u, limit)) bad = true;
+    float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)s * 3 * arr);
+    float4 *as = rs + arr / 4;
+    const float4 *ps = rs + 2 * (arr / 4);
+    const int zr = z0 - 1 + j;
+    const int gz = halo_index(zr, nz, G.pz);
+    const int wz = gz >= 0 ? 9 * wall_count(gz, nz, G.pz) : 0;
+    const int nel = rows * nxv;
+    if (G.px && G.py && wz == 0) {
+      for (int e = tid; e < nel; e += TNT) {
+        float4 r = rs[e];
+        if (lag) {
+          const float4 a = as[e];
+          r.x = fmaf(-alpha, a.x, r.x);
+          r.y = fmaf(-alpha, a.y, r.y);
+          r.z = fmaf(-alpha, a.z, r.z);
+          r.w = fmaf(-alpha, a.w, r.w);
+          rs[e] = r;
+        }
+        float4 p = r;
+        if (!first) {
+          const float4 q = ps[e];
+          p.x = fmaf(beta, q.x, r.x);
+          p.y = fmaf(beta, q.y, r.y);
+          p.z = fmaf(beta, q.z, r.z);
+          p.w = fmaf(beta, q.w, r.w);
+        }
+        as[e] = p;
+      }
+    } else {
+      for (int e = tid; e < nel; e += TNT) {
+        const int row = e / nxv, c4 = e - row * nxv;
+        const int gy = halo_index(y0 - 1 + row, ny, G.py);
+        const int wy = gy >= 0 ? 3 * wall_count(gy, ny, G.py) : 0;
+        const int xb = 4 * c4;
+        float4 r = rs[e];
+        if (lag) {
+          const float4 a = as[e];
+          r.x = fmaf(-alpha, a.x, r.x);
+          r.y = fmaf(-alpha, a.y, r.y);
+          r.z = fmaf(-alpha, a.z, r.z);
+          r.w = fmaf(-alpha, a.w, r.w);
+          rs[e] = r;
+        }
+        float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (!first) q = ps[e];
+        float4 p;
+        const float *rr_ = reinterpret_cast<const float *>(&r);
+        const float *qq = reinterpret_cast<const float *>(&q);
+        float *pp = reinterpret_cast<float *>(&p);
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          const int cls = wall_count(xb + i, nx, G.px) + wy + wz;
+          const float zv = cls ? rr_[i] * s_inv[cls] : rr_[i];
+          pp[i] = first ? zv : fmaf(beta, qq[i], zv);
+        }
+        as[e] = p;
+      }
+    }
+  };
+
+  int orow[NPT], oc4[NPT];
+#pragma unroll
+  for (int k = 0; k < NPT; k++) {
+    const int e = tid + k * TNT;
+    orow[k] = e / nxv;
+    oc4[k] = e - orow[k] * nxv;
+  }
+  uchar4 mkA[NPT], mkB[NPT];
+  float4 xvA[NPT], xvB[NPT];
+  auto fetch = [&](int zc, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
+#pragma unroll
+    for (int k = 0; k < NPT; k++) {
+      const unsigned int c = plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + orow[k]) + 4u * oc4[k];
+      if (MASK) {
+        const unsigned int m = ld_u32_pol(mask + c, pol_mask);
+        mk[k] = make_uchar4(m & 0xffu, (m >> 8) & 0xffu, (m >> 16) & 0xffu, m >> 24);
+      }
+      if (lag) xv[k] = ld4_pol(reinterpret_cast<const float4 *>(x + c), pol_stream);
+    }
+  };
+
+  // partial sums: (p,Ap), (r,r), wall part of (r,z) - (r,r), (Ap,z), (Ap,Ap/dL)
+  float s_pap = 0.f, s_rr = 0.f, s_corr = 0.f, s_c1 = 0.f, s_c2 = 0.f;
+  auto stencil = [&](int j, const uchar4 (&mk)[NPT], const float4 (&xv)[NPT]) {
+    const int zc = z0 - 1 + j;
+    const float *cr = stage + (size_t)(j % ns) * 3 * arr;      // r_new, plane z
+    const float *cs = cr + arr;                                 // p_new, plane z
+    const float *ts = stage + (size_t)((j + 1) % ns) * 3 * arr + arr;
+    const float *bs = stage + (size_t)((j - 1 + ns) % ns) * 3 * arr + arr;
+    const float *po = cr + 2 * arr;                             // p_old, plane z
+    const int wz = 9 * wall_count(zc, nz, G.pz);
+    const bool interior = G.px && G.py && wz == 0;
+#pragma unroll
+    for (int k = 0; k < NPT; k++) {
+      const int row = orow[k], c4 = oc4[k];
+      const int off = (row + 1) * nx + 4 * c4;
+      const float4 c = *reinterpret_cast<const float4 *>(cs + off);
+      const float4 n = *reinterpret_cast<const float4 *>(cs + off + nx);
+      const float4 s = *reinterpret_cast<const float4 *>(cs + off - nx);
+      const float4 t = *reinterpret_cast<const float4 *>(ts + off);
+      const float4 b = *reinterpret_cast<const float4 *>(bs + off);
+      float w = __shfl_up_sync(0xffffffffu, c.w, 1);
+      float ea = __shfl_down_sync(0xffffffffu, c.x, 1);
+      if (lane == 0 || c4 == 0) {
+        const int xw = 4 * c4 - 1;
+        w = xw >= 0 ? cs[off - 1] : (G.px ? cs[(row + 1) * nx + nx - 1] : 0.f);
+      }
+      if (lane == 31 || c4 == nxv - 1) {
+        const int xe = 4 * c4 + 4;
+        ea = xe < nx ? cs[off + 4] : (G.px ? cs[(row + 1) * nx] : 0.f);
+      }
+      float a[4];
+      int cls[4] = {0, 0, 0, 0};
+      if (interior) {
+        a[0] = apply_L<float, ISO>(G, s_dL, 0, c.x, c.y, w, n.x, s.x, t.x, b.x);
+        a[1] = apply_L<float, ISO>(G, s_dL, 0, c.y, c.z, c.x, n.y, s.y, t.y, b.y);
+        a[2] = apply_L<float, ISO>(G, s_dL, 0, c.z, c.w, c.y, n.z, s.z, t.z, b.z);
+        a[3] = apply_L<float, ISO>(G, s_dL, 0, c.w, ea, c.z, n.w, s.w, t.w, b.w);
+      } else {
+        const int wy = 3 * wall_count(y0 + row, ny, G.py) + wz;
+        const int xb = 4 * c4;
+#pragma unroll
+        for (int i = 0; i < 4; i++) cls[i] = wall_count(xb + i, nx, G.px) + wy;
+        a[0] = apply_L<float, ISO>(G, s_dL, cls[0], c.x, c.y, w, n.x, s.x, t.x, b.x);
+        a[1] = apply_L<float, ISO>(G, s_dL, cls[1], c.y, c.z, c.x, n.y, s.y, t.y, b.y);
+        a[2] = apply_L<float, ISO>(G, s_dL, cls[2], c.z, c.w, c.y, n.z, s.z, t.z, b.z);
+        a[3] = apply_L<float, ISO>(G, s_dL, cls[3], c.w, ea, c.z, n.w, s.w, t.w, b.w);
+      }
+      if (MASK) {
+        if (mk[k].x) a[0] = 0.f;
+        if (mk[k].y) a[1] = 0.f;
+        if (mk[k].z) a[2] = 0.f;
+        if (mk[k].w) a[3] = 0.f;
+      }
+      const float4 r = *reinterpret_cast<const float4 *>(cr + off);
+      const float rv[4] = {r.x, r.y, r.z, r.w};
+      const float pv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        s_pap = fmaf(pv[i], a[i], s_pap);
+        s_rr = fmaf(rv[i], rv[i], s_rr);
+        if (interior) {
+          s_c1 = fmaf(a[i], rv[i], s_c1);
+          s_c2 = fmaf(a[i], a[i], s_c2);
+        } else {
+          const float iv = cls[i] ? s_inv[cls[i]] : 1.f;
+          s_corr = fmaf((iv - 1.f) * rv[i], rv[i], s_corr);
+          s_c1 = fmaf(a[i], rv[i] * iv, s_c1);
+          s_c2 = fmaf(a[i] * iv, a[i], s_c2);
+        }
+      }
+      const unsigned int g = plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + row) + 4u * c4;
+      st4_pol(reinterpret_cast<float4 *>(Apout + g), make_float4(a[0], a[1], a[2], a[3]), pol_n);
+      st4_pol(reinterpret_cast<float4 *>(pnew + g), c, pol_stream);
+      st4_pol(reinterpret_cast<float4 *>(rout + g), r, pol_n);
+      if (lag) {
+        const float4 q = *reinterpret_cast<const float4 *>(po + off);
+        float4 xo = xv[k];
+        xo.x = fmaf(alpha, q.x, xo.x);
+        xo.y = fmaf(alpha, q.y, xo.y);
+        xo.z = fmaf(alpha, q.z, xo.z);
+        xo.w = fmaf(alpha, q.w, xo.w);
+        st4_pol(reinterpret_cast<float4 *>(x + g), xo, pol_stream);
+      }
+    }
+  };
+
+  if (tid == 0) {
+    const int pre = min(ns, np);
+    for (int j = 0; j < pre; j++) issue(j);
+  }
+  const int nj = z1 - z0;
+  fetch(z0, mkA, xvA);
+  if (nj >= 2) fetch(z0 + 1, mkB, xvB);
+  prep(0);
+  prep(1);
+  auto step = [&](int j, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
+    prep(j + 1);
+    fence_proxy_async();
+    __syncthreads();
+    if (tid == 0 && j >= 2 && j - 2 + ns < np) issue(j - 2 + ns);
+    stencil(j, mk, xv);
+    if (j + 2 <= nj) fetch(z0 + j + 1, mk, xv);
+  };
+  for (int j = 1; j <= nj; j += 2) {
+    step(j, mkA, xvA);
+    if (j + 1 <= nj) step(j + 1, mkB, xvB);
+  }
+
+  if (__syncthreads_or(bad)) {
+    if (tid == 0) {
+      for (int j = max(0, np - ns); j < np; j++) mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u, limit);
+      atomicExch(&st->done, (int)DONE_TIMEOUT);
+    }
+    return;
+  }
+  double v[5] = {(double)s_pap, (double)s_rr + (double)s_corr, (double)s_rr, (double)s_c1, (double)s_c2}, tot[5];
+  const unsigned int nb = gridDim.x * gridDim.y;
+  const unsigned int bid = blockIdx.x + gridDim.x * blockIdx.y;
+  if (last_cta_reduce<5>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
+    st->fq += 1;
+    if (lag) finish_deferred(st, tot[1], tot[2]);  // r_{q-1} ends iteration q - 1
+    st->dlag = 0;  // the pending step is in x and r now
+    // the step of this kernel's direction stays pending (also when the
+    // recursive residual has met TRUE_REL: the confirmation folds it in)
+    if (st->done == RUNNING || st->done == DONE_PENDING) {
+      const double rz = st->rz, pap = tot[0];
+      const double a = rz / pap;
+      st->pAp = pap;
+      st->alpha = a;
+      st->beta = (rz - 2.0 * a * tot[3] + a * a * tot[4]) / rz;
+      st->first = 0;
+      st->dlag = 1;
+      decide_replacement(st);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ host --
 namespace {
 
@@ -424,6 +738,7 @@ constexpr int kMaxStageBytes = 200 * 1024;
 template <int NPT, bool MASK, bool ISO>
 void set_smem_attr() {
   cudaFuncSetAttribute(k1_tma<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes);
+  cudaFuncSetAttribute(k1_fused<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes);
 }
 
 int env_int(const char *name, int dflt) {
@@ -440,6 +755,10 @@ struct bbpp_tma_state {
   bool ok = false;
   int ty = 0, npt = 0, ns = 0, kz = 0, four_d = 0, smem = 0;
   dim3 grid;
+  // the fused iteration kernel: three staged arrays, its own wave
+  bool fok = false;
+  int fkz = 0, fsmem = 0;
+  dim3 fgrid;
   std::vector<MapPair> maps;
 };
 
@@ -501,14 +820,33 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
   cudaGetLastError();
   if (per_sm < 1) return;
   const int slabs = ny / ty;
-  const long long target = (long long)ctx->sms * per_sm;
-  int nzc = (int)std::max<long long>(1, target / slabs);
-  nzc = std::min(nzc, nz);
-  int kz = (nz + nzc - 1) / nzc;
-  nzc = (nz + kz - 1) / kz;
-  t->kz = kz;
-  t->grid = dim3(slabs, nzc, 1);
+  auto chunking = [&](int per, int *kz_out, dim3 *grid_out) {
+    const long long target = (long long)ctx->sms * per;
+    int nzc = (int)std::max<long long>(1, target / slabs);
+    nzc = std::min(nzc, nz);
+    const int kz = (nz + nzc - 1) / nzc;
+    nzc = (nz + kz - 1) / kz;
+    *kz_out = kz;
+    *grid_out = dim3(slabs, nzc, 1);
+  };
+  chunking(per_sm, &t->kz, &t->grid);
   t->ok = true;
+  // fused kernel: r, Ap_old and p_old staged (three arrays per stage)
+  const int fsmem = ns * 3 * (ty + 2) * nx * 4;
+  int fper = 0;
+  if (fsmem <= kMaxStageBytes) {
+#define BBPP_FUSED_OCC(N) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fper, k1_fused<N, true, true>, TNT, fsmem);
+    if (npt == 1) { BBPP_FUSED_OCC(1) }
+    else if (npt == 2) { BBPP_FUSED_OCC(2) }
+    else { BBPP_FUSED_OCC(4) }
+#undef BBPP_FUSED_OCC
+    cudaGetLastError();
+  }
+  if (fper >= 1) {
+    t->fsmem = fsmem;
+    chunking(fper, &t->fkz, &t->fgrid);
+    t->fok = true;
+  }
 }
 
 void bbpp_tma_free(bbpp_ctx *ctx) {
@@ -525,8 +863,14 @@ bool bbpp_tma_chunks(const bbpp_ctx *ctx, int *kz, int *nzc) {
 }
 
 size_t bbpp_tma_partials(const bbpp_ctx *ctx) {
-  return (ctx->tma && ctx->tma->ok) ? (size_t)ctx->tma->grid.x * ctx->tma->grid.y : 0;
+  if (!ctx->tma || !ctx->tma->ok) return 0;
+  size_t n = (size_t)ctx->tma->grid.x * ctx->tma->grid.y;
+  // the fused kernel sums five products per CTA into room for three per CTA
+  if (ctx->tma->fok) n = std::max(n, ((size_t)ctx->tma->fgrid.x * ctx->tma->fgrid.y * 5 + 2) / 3);
+  return n;
 }
+
+bool bbpp_tma_fused_ok(const bbpp_ctx *ctx) { return ctx->tma && ctx->tma->ok && ctx->tma->fok; }
 
 // tensor maps of one vector (copied out: the cache may reallocate)
 static bool get_maps(bbpp_tma_state *t, const float *p, const GeoL &G, MapPair *out) {
@@ -541,6 +885,50 @@ static bool get_maps(bbpp_tma_state *t, const float *p, const GeoL &G, MapPair *
   if (t->maps.size() >= 16) t->maps.erase(t->maps.begin());
   t->maps.push_back(m);
   *out = m;
+  return true;
+}
+
+// tensor maps of the six buffers of a fused solve, built before its graphs
+bool bbpp_tma_fused_maps(bbpp_ctx *ctx, const float *const r[2], const float *const a[2], const float *const p[2]) {
+  bbpp_tma_state *t = ctx->tma;
+  if (!t || !t->ok || !t->fok) return false;
+  MapPair m;
+  for (int i = 0; i < 2; i++)
+    if (!get_maps(t, r[i], ctx->GL, &m) || !get_maps(t, a[i], ctx->GL, &m) || !get_maps(t, p[i], ctx->GL, &m))
+      return false;
+  return true;
+}
+
+bool bbpp_tma_fused(bbpp_ctx *ctx, const uint8_t *mask, const float *rin, const float *apin, const float *pold,
+                    float *rout, float *pnew, float *apout, float *x, DevState *st) {
+  bbpp_tma_state *t = ctx->tma;
+  if (!t || !t->ok || !t->fok) return false;
+  MapPair mr, ma, mp;
+  if (!get_maps(t, rin, ctx->GL, &mr) || !get_maps(t, apin, ctx->GL, &ma) || !get_maps(t, pold, ctx->GL, &mp))
+    return false;
+  FusedMaps M;
+  M.r_rows = mr.rows;
+  M.r_row = mr.row;
+  M.a_rows = ma.rows;
+  M.a_row = ma.row;
+  M.p_rows = mp.rows;
+  M.p_row = mp.row;
+#define BBPP_FUSED_LAUNCH(N, MK, IS)                                                                             \
+  bbpp_launch(ctx, k1_fused<N, MK, IS>, t->fgrid, dim3(TNT), (size_t)t->fsmem, ctx->GL, M, rout, pnew, apout, x, \
+              mask, st, ctx->partials, t->ty, t->fkz, t->ns, t->four_d, (int)ctx->l2hint)
+#define BBPP_FUSED_NPT(N)                              \
+  if (mask) {                                          \
+    if (ctx->GL.iso) BBPP_FUSED_LAUNCH(N, true, true);   \
+    else BBPP_FUSED_LAUNCH(N, true, false);              \
+  } else {                                             \
+    if (ctx->GL.iso) BBPP_FUSED_LAUNCH(N, false, true);  \
+    else BBPP_FUSED_LAUNCH(N, false, false);             \
+  }
+  if (t->npt == 1) { BBPP_FUSED_NPT(1) }
+  else if (t->npt == 2) { BBPP_FUSED_NPT(2) }
+  else { BBPP_FUSED_NPT(4) }
+#undef BBPP_FUSED_NPT
+#undef BBPP_FUSED_LAUNCH
   return true;
 }
 
