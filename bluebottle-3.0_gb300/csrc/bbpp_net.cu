@@ -553,86 +553,131 @@ __global__ void k_guess_out(const float *__restrict__ out, const double *__restr
     x[i] = (mask && mask[i]) ? 0.0 : (prev ? prev[i] : 0.0) + (double)out[i] * sr;
 }
 
-// Restriction by 2 (cell-centred): r and p_prev become the means of the
-// 2x2x2 children; a coarse cell is solid when at least 4 of its children are.
-__global__ void k_restrict2(const double *__restrict__ r, const double *__restrict__ p,
-                            const uint8_t *__restrict__ mask, int nx, int ny, int nz, double *__restrict__ rc,
-                            double *__restrict__ pc, uint8_t *__restrict__ mc) {
-  const int cx = nx >> 1, cy = ny >> 1;
-  const long long nc = (long long)cx * cy * (nz >> 1);
-  for (long long e = blockIdx.x * 256LL + threadIdx.x; e < nc; e += (long long)gridDim.x * 256) {
-    const int i = (int)(e % cx);
-    const long long t = e / cx;
-    const int j = (int)(t % cy), k = (int)(t / cy);
-    double sr = 0.0, sp = 0.0;
+// The warm start's residual r = rhs - (-A) p_prev, restricted by 2 in the same
+// pass (cell-centred: the means of the 2x2x2 children), with p_prev's means
+// and the coarse solid cells (at least 4 solid children).  The residual is
+// formed as in the residual kernel (k_resid: neighbours of or across solid
+// cells count 0, walls through the class diagonal) but in FP32 arithmetic: it
+// only feeds the BF16 network.  prev == NULL: r = rhs, p_prev = 0.
+__global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, const double *__restrict__ rhs,
+                                                         const double *__restrict__ prev,
+                                                         const uint8_t *__restrict__ mask, double *__restrict__ rc,
+                                                         double *__restrict__ pc, uint8_t *__restrict__ mc) {
+  __shared__ float s_tab[81];
+  for (int e = threadIdx.x; e < 81; e += blockDim.x) s_tab[e] = (float)G.tab[e];
+  __syncthreads();
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const unsigned int cxn = (unsigned)nx >> 1, cyn = (unsigned)ny >> 1;
+  const unsigned int nc = cxn * cyn * ((unsigned)nz >> 1);
+  const float fx = (float)G.cx, fy = (float)G.cy, fz = (float)G.cz;
+  // p_prev at a neighbour (0 outside a wall); solid: the neighbour is solid
+  auto nb = [&](int xx, int yy, int zz, bool &solid) -> float {
+    const int gx = bbpp::halo_index(xx, nx, G.px), gy = bbpp::halo_index(yy, ny, G.py),
+              gz = bbpp::halo_index(zz, nz, G.pz);
+    solid = false;
+    if (gx < 0 || gy < 0 || gz < 0) return 0.f;
+    const unsigned int c = (unsigned)gx + (unsigned)nx * ((unsigned)gy + (unsigned)ny * (unsigned)gz);
+    if (mask) solid = mask[c] != 0;
+    return (float)prev[c];
+  };
+  for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < nc; e += gridDim.x * 256u) {
+    const unsigned int i = e % cxn, t = e / cxn, j = t % cyn, k = t / cyn;
+    float sr = 0.f, sp = 0.f;
     int sm = 0;
 #pragma unroll
-    for (int dz = 0; dz < 2; dz++)
-#pragma unroll
-      for (int dy = 0; dy < 2; dy++) {
-        const long long b = ((long long)(2 * k + dz) * ny + (2 * j + dy)) * nx + 2 * i;
-        sr += r[b] + r[b + 1];
-        if (p) sp += p[b] + p[b + 1];
-        if (mask) sm += (mask[b] != 0) + (mask[b + 1] != 0);
+    for (int ch = 0; ch < 8; ch++) {
+      const int x = 2 * (int)i + (ch & 1), y = 2 * (int)j + ((ch >> 1) & 1), z = 2 * (int)k + (ch >> 2);
+      const unsigned int c = (unsigned)x + (unsigned)nx * ((unsigned)y + (unsigned)ny * (unsigned)z);
+      const bool ms = mask && mask[c] != 0;
+      float r = (float)rhs[c];
+      if (prev) {
+        const float pcv = (float)prev[c];
+        bool s0, s1, s2, s3, s4, s5;
+        float pe = nb(x + 1, y, z, s0), pw = nb(x - 1, y, z, s1), pn = nb(x, y + 1, z, s2), ps = nb(x, y - 1, z, s3);
+        float pt = nb(x, y, z + 1, s4), pb = nb(x, y, z - 1, s5);
+        if (mask) {
+          pe = (ms || s0) ? 0.f : pe;
+          pw = (ms || s1) ? 0.f : pw;
+          pn = (ms || s2) ? 0.f : pn;
+          ps = (ms || s3) ? 0.f : ps;
+          pt = (ms || s4) ? 0.f : pt;
+          pb = (ms || s5) ? 0.f : pb;
+        }
+        const int cls = bbpp::wall_count(x, nx, G.px) + 3 * bbpp::wall_count(y, ny, G.py) +
+                        9 * bbpp::wall_count(z, nz, G.pz);
+        const float d = ms ? s_tab[54 + cls] : s_tab[cls];
+        float s_ = fx * (pe + pw);
+        s_ = fmaf(fy, pn + ps, s_);
+        s_ = fmaf(fz, pt + pb, s_);
+        r -= fmaf(d, pcv, -s_);
+        sp += pcv;
       }
-    rc[e] = 0.125 * sr;
-    pc[e] = 0.125 * sp;
+      sr += r;
+      sm += ms ? 1 : 0;
+    }
+    rc[e] = 0.125 * (double)sr;
+    pc[e] = 0.125 * (double)sp;
     mc[e] = sm >= 4 ? 1 : 0;
   }
 }
 
+// the coarse correction p0c - pc (0 on coarse solid cells), in place of p0c
+__global__ void k_corr2(double *__restrict__ p0c, const double *__restrict__ pc, const uint8_t *__restrict__ mc,
+                        unsigned int nc) {
+  for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < nc; e += gridDim.x * 256u)
+    p0c[e] = mc[e] ? 0.0 : p0c[e] - pc[e];
+}
+
 // one axis of the cell-centred trilinear prolongation by 2: fine cell a lies
 // at coarse coordinate a/2 - 1/4, between coarse cells lo and hi, hi weighted w
-__device__ __forceinline__ void prolong_axis(int a, int n, int periodic, int &lo, int &hi, double &w) {
+__device__ __forceinline__ void prolong_axis(int a, int n, int periodic, int &lo, int &hi, float &w) {
   const int m = a >> 1;
   if (a & 1) {
     lo = m;
     hi = m + 1;
-    w = 0.25;
+    w = 0.25f;
   } else {
     lo = m - 1;
     hi = m;
-    w = 0.75;
+    w = 0.75f;
   }
   if (periodic) {
-    lo = (lo + n) % n;
-    hi = hi % n;
+    lo = lo < 0 ? lo + n : lo;
+    hi = hi >= n ? hi - n : hi;
   } else {
     lo = max(lo, 0);
     hi = min(hi, n - 1);
   }
 }
 
-// x = p_prev + the trilinear interpolation of the coarse correction
-// p0c - pc (0 on coarse solid cells); fine solid cells 0, as the fine path.
-__global__ void k_prolong2(const double *__restrict__ p0c, const double *__restrict__ pc,
-                           const uint8_t *__restrict__ mc, const double *__restrict__ prev,
-                           const uint8_t *__restrict__ mask, int nx, int ny, int nz, int px, int py, int pz,
-                           double *__restrict__ x) {
-  const int cx = nx >> 1, cy = ny >> 1, cz = nz >> 1;
-  const long long n = (long long)nx * ny * nz;
-  for (long long f = blockIdx.x * 256LL + threadIdx.x; f < n; f += (long long)gridDim.x * 256) {
+// x = p_prev + the trilinear interpolation of the coarse correction; fine
+// solid cells 0, as the guess on the grid itself
+__global__ void __launch_bounds__(256) k_prolong2(const double *__restrict__ corr, const double *__restrict__ prev,
+                                                  const uint8_t *__restrict__ mask, int nx, int ny, int nz, int px,
+                                                  int py, int pz, double *__restrict__ x) {
+  const int cxn = nx >> 1, cyn = ny >> 1, czn = nz >> 1;
+  const unsigned int n = (unsigned)nx * (unsigned)ny * (unsigned)nz;
+  for (unsigned int f = blockIdx.x * 256u + threadIdx.x; f < n; f += gridDim.x * 256u) {
     if (mask && mask[f]) {
       x[f] = 0.0;
       continue;
     }
-    const int i = (int)(f % nx);
-    const long long t = f / nx;
-    const int j = (int)(t % ny), k = (int)(t / ny);
+    const unsigned int t = f / (unsigned)nx;
+    const int i = (int)(f - t * (unsigned)nx);
+    const int k = (int)(t / (unsigned)ny), j = (int)(t - (unsigned)k * (unsigned)ny);
     int xl, xh, yl, yh, zl, zh;
-    double wx, wy, wz;
-    prolong_axis(i, cx, px, xl, xh, wx);
-    prolong_axis(j, cy, py, yl, yh, wy);
-    prolong_axis(k, cz, pz, zl, zh, wz);
-    double v = 0.0;
-#pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const int zz = (c & 4) ? zh : zl, yy = (c & 2) ? yh : yl, xx = (c & 1) ? xh : xl;
-      const double w = ((c & 4) ? wz : 1.0 - wz) * ((c & 2) ? wy : 1.0 - wy) * ((c & 1) ? wx : 1.0 - wx);
-      const long long e = ((long long)zz * cy + yy) * cx + xx;
-      v += mc[e] ? 0.0 : w * (p0c[e] - pc[e]);
-    }
-    x[f] = (prev ? prev[f] : 0.0) + v;
+    float wx, wy, wz;
+    prolong_axis(i, cxn, px, xl, xh, wx);
+    prolong_axis(j, cyn, py, yl, yh, wy);
+    prolong_axis(k, czn, pz, zl, zh, wz);
+    const unsigned int r00 = ((unsigned)zl * cyn + yl) * cxn, r01 = ((unsigned)zl * cyn + yh) * cxn;
+    const unsigned int r10 = ((unsigned)zh * cyn + yl) * cxn, r11 = ((unsigned)zh * cyn + yh) * cxn;
+    const float a00 = (1.f - wx) * (float)corr[r00 + xl] + wx * (float)corr[r00 + xh];
+    const float a01 = (1.f - wx) * (float)corr[r01 + xl] + wx * (float)corr[r01 + xh];
+    const float a10 = (1.f - wx) * (float)corr[r10 + xl] + wx * (float)corr[r10 + xh];
+    const float a11 = (1.f - wx) * (float)corr[r11 + xl] + wx * (float)corr[r11 + xh];
+    const float v = (1.f - wz) * ((1.f - wy) * a00 + wy * a01) + wz * ((1.f - wy) * a10 + wy * a11);
+    x[f] = (prev ? prev[f] : 0.0) + (double)v;
   }
 }
 
@@ -1252,10 +1297,11 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
   cudaStream_t saved = n->stream;
   n->stream = ctx->stream;
   cudaEventRecord(e0, ctx->stream);
-  // residual of the warm start into the solver's free Ap buffer
+  // residual of the warm start into the solver's free Ap buffer (the coarse
+  // path forms it inside its restriction)
   const double *r = rhs;
   int rc = 0;
-  if (prev) {
+  if (prev && f == 1) {
     rc = bbpp_residual_async(ctx, mask, rhs, prev, ctx->Ap);
     r = ctx->Ap;
   }
@@ -1265,20 +1311,21 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
     NetWork *w = ctx->net;
     const long long nc = (long long)(nx / 2) * (ny / 2) * (nz / 2);
     if (rc == 0) {
-      k_restrict2<<<nblocks(nc), 256, 0, ctx->stream>>>(r, prev, mask, nx, ny, nz, w->rc, w->pc, w->mc);
+      k_resid_restrict2<<<nblocks(nc), 256, 0, ctx->stream>>>(ctx->G, rhs, prev, mask, w->rc, w->pc, w->mc);
       if (cudaGetLastError() != cudaSuccess) rc = BBPP_CUDA_ERROR;
     }
     if (rc == 0) rc = bbpp_net_infer(n, nx / 2, ny / 2, nz / 2, 4.0 * h2, w->rc, w->pc, mask ? w->mc : nullptr, w->p0c);
     if (rc == 0) {
-      k_prolong2<<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->p0c, w->pc, w->mc, prev, mask, nx, ny, nz, ctx->G.px,
-                                                              ctx->G.py, ctx->G.pz, x);
+      k_corr2<<<nblocks(nc), 256, 0, ctx->stream>>>(w->p0c, w->pc, w->mc, (unsigned)nc);
+      k_prolong2<<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->p0c, prev, mask, nx, ny, nz, ctx->G.px, ctx->G.py,
+                                                              ctx->G.pz, x);
       if (cudaGetLastError() != cudaSuccess) rc = BBPP_CUDA_ERROR;
     }
-    ctx->launches += 2;
+    ctx->launches += 3;
   } else if (rc == 0) {
     rc = bbpp_net_infer(n, nx, ny, nz, h2, r, prev, mask, x);
   }
-  ctx->launches += (n->launches - l0) + (prev ? 1 : 0);
+  ctx->launches += (n->launches - l0) + (prev && f == 1 ? 1 : 0);
   cudaEventRecord(e1, ctx->stream);
   n->stream = saved;
   if (rc == 0) {
