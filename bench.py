@@ -33,10 +33,11 @@ WORKLOAD = ("C3: 256^3 cells, periodic x/y + Neumann z, 1000 spheres r=6 cells, 
 # sample of the reference arm to a full solve.
 C3_FP64_ITERS = 604
 # DRAM bytes (read + write) per launch of the dominant kernels on this workload,
-# from one ncu capture each (profiles/k1_tma_k2_update_f32_c3_256.md,
-# profiles/k1_search2_k2_update_f64_c3_256.md): kernel kind -> bytes
+# from one ncu capture each (--set full, two launches of a 256^3 solve; the
+# summaries sit with the other profiles): kernel kind -> bytes
 NCU_TRAFFIC = {"search_spmv_f32": 226.697984e6 + 150.230784e6, "search_spmv": 433.925632e6 + 353.379328e6,
-               "update_f32": 134.251008e6 + 20.922112e6, "update": 268.485376e6 + 92.526592e6}
+               "update_f32": 134.251008e6 + 20.922112e6, "update": 268.485376e6 + 92.526592e6,
+               "fused_f32": 305.875968e6 + 215.252224e6}
 
 
 def peaks():
