@@ -1267,6 +1267,12 @@ void bbpp_rec_collect(bbpp_ctx *ctx, std::vector<KEv> &evs, int iters_done, bool
   }
 }
 
+extern "C" int bbpp_set_fused(bbpp_ctx *ctx, int on) {
+  if (!ctx || (on != 0 && on != 1)) return BBPP_BAD_ARG;
+  ctx->fused = on == 1;
+  return 0;
+}
+
 extern "C" int bbpp_set_profiling(bbpp_ctx *ctx, int on) {
   if (!ctx) return BBPP_BAD_ARG;
   if ((on != 0) != ctx->profiling) drop_graphs(ctx);

@@ -203,6 +203,10 @@ int bbpp_kernel_stats(bbpp_ctx *ctx, bbpp_kstat *out, int max, int *n);
 /* Enable (1) or disable (0) per-kernel CUDA-event timing and reset the
  * counters; events are captured between the kernels of the graphs. */
 int bbpp_set_profiling(bbpp_ctx *ctx, int on);
+/* The FP32 iteration of reliable-update solves: 1 = one fused kernel per
+ * iteration (the default where the TMA kernels take the grid), 0 = a search
+ * kernel and an update kernel. */
+int bbpp_set_fused(bbpp_ctx *ctx, int on);
 
 /* ---- learned initial guess (no counterpart in the reference) ----
  * A 3-level 3D conv encoder-decoder (channels 16/32/64, 3x3x3 kernels, BF16

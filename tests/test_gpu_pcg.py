@@ -175,6 +175,38 @@ def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol, ir_mode):
     assert err < 1e4 * tol, err
 
 
+# grids the TMA kernels take (nx in 32 .. 256, a power of two), where the fused form exists
+@pytest.mark.parametrize("name,n,bc", [("C3", 64, None), ("C2", 128, None), ("C1", 32, None), ("C3", 64, "nnn"),
+                                       ("C3", 64, "pnp")])
+def test_fused_iteration_matches_two_kernels(lib, orc, name, n, bc):
+    """The fused FP32 iteration (pending update and search step in one kernel,
+    beta from the one-step expansion) against the search + update kernels:
+    the same PCG iterations within a few, both at the tolerance, the same
+    solution to well within the tolerance's reach."""
+    g, mask, rhs, _ = problems.make_problem(name, n=n)
+    if bc is not None:
+        g = problems.make_grid(n, bc)
+    s = bbpp.Solver(g)
+    out = {}
+    for fused in (True, False):
+        s.set_fused(fused)
+        out[fused] = s.solve_host(rhs, mask, tol=1e-8, precision=bbpp.FP32_IR)
+    (xf, rf), (x2, r2) = out[True], out[False]
+    for rep in (rf, r2):
+        assert rep.status == bbpp.CONVERGED and rep.true_rel <= 1e-8 * 1.01
+    assert abs(rf.iters - r2.iters) <= max(3, r2.iters // 50)
+    if mask is None:
+        xf, x2 = xf - xf.mean(), x2 - x2.mean()
+    assert np.abs(xf - x2).max() <= 1e-5 * np.abs(x2).max()
+    # the fused path ran: its kernel appears in the kernel statistics
+    s.set_fused(True)
+    s.set_profiling(True)
+    s.solve_host(rhs, mask, tol=1e-8, precision=bbpp.FP32_IR)
+    kinds = {k[0] for k in s.kernel_stats()}
+    s.set_profiling(False)
+    assert "fused_f32" in kinds
+
+
 @pytest.mark.parametrize("dims,bc", SHAPES)
 @pytest.mark.parametrize("precision,ir_mode", [(bbpp.FP64, 0), (bbpp.FP32_IR, bbpp.IR_RELIABLE),
                                                (bbpp.FP32_IR, bbpp.IR_RESTART)])
