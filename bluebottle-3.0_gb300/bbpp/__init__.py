@@ -128,6 +128,7 @@ def lib():
         "bbpp_kernel_stats": (I, [P, P, I, ctypes.POINTER(I)]),
         "bbpp_set_profiling": (I, [P, I]),
         "bbpp_set_fused": (I, [P, I]),
+        "bbpp_set_ff_resid": (I, [P, I]),
         "bbpp_rng_uniform": (None, [ctypes.c_ulonglong, ctypes.c_longlong, D, D, P]),
         "bbpp_rng_gauss": (None, [ctypes.c_ulonglong, ctypes.c_longlong, P]),
         "bbpp_version": (ctypes.c_char_p, []),
@@ -295,6 +296,10 @@ class Solver:
     def set_fused(self, on):
         """FP32 reliable-update iterations as one fused kernel (True) or two."""
         _check(lib().bbpp_set_fused(self.handle, 1 if on else 0))
+
+    def set_ff_resid(self, on):
+        """Reliable-update residuals in float-float (True) or FP64 arithmetic."""
+        _check(lib().bbpp_set_ff_resid(self.handle, 1 if on else 0))
 
     def kernel_stats(self):
         arr = (KStat * 32)()

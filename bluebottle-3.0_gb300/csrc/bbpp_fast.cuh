@@ -605,6 +605,8 @@ __global__ void __launch_bounds__(FNT) k_settle(const GeoL G, T *__restrict__ x,
 }
 
 // --------------------------------------------------------------- residual --
+__device__ __forceinline__ void resid_finish(DevState *st, const double (&tot)[3], int mode);
+
 // r = bscale rhs - L x on fluid cells, r = 0 (and x = 0 with zero_solid_x) on
 // solid cells.  TXT: type of x and rhs, TR: type of r.  Dots in FP64 of the
 // stored r: (r,z), (r,r); and (rhs,rhs) of the unscaled rhs.
@@ -696,7 +698,14 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
   double v[3] = {rr + corr, rr, bb}, tot[3];
   const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
   const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  if (last_cta_reduce<3>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
+  if (last_cta_reduce<3>(v, partials, st, nb, bid, s_red, tot) && tid == 0) resid_finish(st, tot, mode);
+}
+
+// The device state after a residual: init (mode 0), replacement at a
+// checkpoint (1) or confirmation of a recursive convergence (2).  tot: (r,z),
+// (r,r), (rhs,rhs).
+__device__ __forceinline__ void resid_finish(DevState *st, const double (&tot)[3], int mode) {
+  {
     const double rz1 = tot[0], rr1 = tot[1];
     if (mode == 0) {  // init: thresholds from (rhs,rhs) of the unscaled rhs
       st->bb = tot[2];
@@ -739,6 +748,144 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       }
     }
   }
+}
+
+// ------------------------------------------------- float-float residual --
+// r = bscale rhs - L x for FP64 x and rhs into an FP32 r, evaluated in
+// float-float arithmetic on the FP32 pipe (GB300 issues FP64 at 1/64 of FP32).
+// A value is an unevaluated sum hi + lo of two floats (about 48 bits); the
+// error-free transformations are Knuth's two-sum and the FMA two-product
+// (Dekker's product with a fused multiply-add), renormalised with
+// Dekker's fast two-sum.  Each FP64 input is split once, when its tile is
+// loaded (one FP64 subtraction).  The error of L x is ~2^-48 |x|, far below
+// what the FP32 residual keeps.  Dots are summed in FP32 per thread and in
+// FP64 across threads, as the iteration kernels do.  Same tiles, masking,
+// wall classes and state updates as k_resid_s.
+struct ff {
+  float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_split(double v) {
+  const float h = __double2float_rn(v);
+  return ff{h, __double2float_rn(v - (double)h)};
+}
+
+__device__ __forceinline__ ff ff_fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return ff_fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.hi, -p);
+  return ff_fast_two_sum(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+
+template <bool MASK, bool ISO>
+__global__ void __launch_bounds__(FNT) k_resid_ff(const GeoL G, double *__restrict__ xin,
+                                                  const double *__restrict__ rhs, float *__restrict__ rout,
+                                                  const uint8_t *__restrict__ mask, DevState *st, double *partials,
+                                                  int kz, int mode, double bscale) {
+  __shared__ ff s_dL[27];
+  __shared__ float s_inv[27];
+  __shared__ ff sp[3][FHY][FHX];
+  __shared__ uint8_t sm[3][FHY][FHX + 2];
+  __shared__ double s_red[3 * FNT / 32];
+  pdl_sync();
+  if (mode == 1 && skip_step(st, 2)) return;
+  for (int e = threadIdx.x; e < 27; e += blockDim.x) {
+    s_dL[e] = ff_split(G.dL[e]);
+    s_inv[e] = G.finvL[e];
+  }
+  const ff ax = ff_split(G.ax), ay = ff_split(G.ay), az = ff_split(G.az), bs = ff_split(bscale);
+  const int tid = threadIdx.x;
+  const int tx = tid & 31, ty = tid >> 5;
+  const int x0 = blockIdx.x * FX, y0 = blockIdx.y * FY;
+  const int z0 = blockIdx.z * kz, z1 = min(z0 + kz, G.nz);
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const long long sxy = (long long)nx * ny;
+  __syncthreads();
+  auto load_plane = [&](int slot, int zr) {
+    const int gz = halo_index(zr, nz, G.pz);
+    for (int e = tid; e < FHE; e += FNT) {
+      const int ly = e / FHX, lx = e - ly * FHX;
+      const int gx = halo_index(x0 + lx - 1, nx, G.px), gy = halo_index(y0 + ly - 1, ny, G.py);
+      ff val = ff{0.f, 0.f};
+      uint8_t m = 0;
+      if (gz >= 0 && gx >= 0 && gy >= 0) {
+        const long long c = gx + (long long)nx * gy + sxy * gz;
+        if (MASK) m = mask[c];
+        if (!m) val = ff_split(xin[c]);  // solid cells count as x = 0
+      }
+      sp[slot][ly][lx] = val;
+      sm[slot][ly][lx] = m;
+    }
+  };
+  float corr = 0.f, rr = 0.f, bb = 0.f;
+  const bool want_bb = mode == 0;
+  load_plane(0, z0 - 1);
+  load_plane(1, z0);
+  const int gx = x0 + tx;
+  auto cell = [&](auto interior_tag, int sb, int sc, int st_, int z) {
+    constexpr bool INTERIOR = decltype(interior_tag)::value;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int gy = y0 + ty + 8 * h;
+      if (gx >= nx || gy >= ny) continue;
+      const int ly = ty + 1 + 8 * h, lx = tx + 1;
+      const bool mc = MASK && sm[sc][ly][lx] != 0;
+      const long long c = gx + (long long)nx * gy + sxy * z;
+      const double bvd = rhs[c];
+      const ff bv = ff_split(bvd);
+      if (want_bb) bb = fmaf(bv.hi, bv.hi, bb);
+      if (mc) {
+        rout[c] = 0.f;
+        if (mode == 0) xin[c] = 0.0;
+        continue;
+      }
+      const ff pc = sp[sc][ly][lx];
+      const ff pe = sp[sc][ly][lx + 1], pw = sp[sc][ly][lx - 1];
+      const ff pn = sp[sc][ly + 1][lx], ps = sp[sc][ly - 1][lx];
+      const ff pt = sp[st_][ly][lx], pb = sp[sb][ly][lx];
+      const int cls = INTERIOR ? 0 : wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py) + 9 * wall_count(z, nz, G.pz);
+      // a = L x at the cell (apply_L's formula, in float-float)
+      ff s;
+      if (ISO) {
+        s = ff_mul(ax, ff_add(ff_add(ff_add(pe, pw), ff_add(pn, ps)), ff_add(pt, pb)));
+      } else {
+        s = ff_add(ff_add(ff_mul(ax, ff_add(pe, pw)), ff_mul(ay, ff_add(pn, ps))), ff_mul(az, ff_add(pt, pb)));
+      }
+      const ff d = cls ? ff_mul(s_dL[cls], pc) : pc;
+      const ff a = ff_add(d, ff_neg(s));
+      const ff r = ff_add(ff_mul(bs, bv), ff_neg(a));
+      const float rv = __fadd_rn(r.hi, r.lo);
+      rout[c] = rv;
+      const float r2 = rv * rv;
+      rr += r2;
+      if (!INTERIOR && cls) corr = fmaf(s_inv[cls] - 1.f, r2, corr);
+    }
+  };
+  for (int z = z0; z < z1; z++) {
+    const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
+    load_plane(st_, z + 1);
+    __syncthreads();
+    if (G.px && G.py && wall_count(z, nz, G.pz) == 0) cell(std::true_type(), sb, sc, st_, z);
+    else cell(std::false_type(), sb, sc, st_, z);
+    __syncthreads();
+  }
+  double v[3] = {(double)rr + (double)corr, (double)rr, (double)bb}, tot[3];
+  const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
+  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (last_cta_reduce<3>(v, partials, st, nb, bid, s_red, tot) && tid == 0) resid_finish(st, tot, mode);
 }
 
 }  // namespace bbpp

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/bbpp.h"
@@ -279,6 +280,9 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
     // one fused kernel per FP32 iteration (BBPP_FUSED=0: search and update kernels)
     const char *fu = getenv("BBPP_FUSED");
     ctx->fused = !(fu && fu[0] == '0');
+    // residuals of FP64 x into FP32 r in float-float arithmetic (BBPP_FF_RESID=0: FP64)
+    const char *ff = getenv("BBPP_FF_RESID");
+    ctx->ff_resid = !(ff && ff[0] == '0');
   }
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
@@ -480,6 +484,28 @@ void bbpp_launch_resid_s(bbpp_ctx *ctx, const uint8_t *mask, TXT *x, const TXT *
   // bytes/cell: read x, rhs (+ mask), write r
   bbpp_rec_begin(ctx, sizeof(TXT) == 8 ? KK_RESID : KK_RESID_F32, 2.0 * sizeof(TXT) + sizeof(TR) + (mask ? 1 : 0));
   const dim3 g = ctx->fgrid, b(FNT);
+  if constexpr (std::is_same<TXT, double>::value && std::is_same<TR, float>::value) {
+    // FP64 x into an FP32 residual: float-float arithmetic on the FP32 pipe
+    if (ctx->ff_resid) {
+      if (mask) {
+        if (ctx->GL.iso)
+          bbpp_launch(ctx, k_resid_ff<true, true>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz, mode,
+                      bscale);
+        else
+          bbpp_launch(ctx, k_resid_ff<true, false>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz,
+                      mode, bscale);
+      } else {
+        if (ctx->GL.iso)
+          bbpp_launch(ctx, k_resid_ff<false, true>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz,
+                      mode, bscale);
+        else
+          bbpp_launch(ctx, k_resid_ff<false, false>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials, ctx->fkz,
+                      mode, bscale);
+      }
+      bbpp_rec_end(ctx);
+      return;
+    }
+  }
   if (mask) {
     if (ctx->GL.iso)
       bbpp_launch(ctx, k_resid_s<TXT, TR, true, true>, g, b, 0, ctx->GL, x, rhs, r, mask, st, ctx->partials,
@@ -1270,6 +1296,13 @@ void bbpp_rec_collect(bbpp_ctx *ctx, std::vector<KEv> &evs, int iters_done, bool
 extern "C" int bbpp_set_fused(bbpp_ctx *ctx, int on) {
   if (!ctx || (on != 0 && on != 1)) return BBPP_BAD_ARG;
   ctx->fused = on == 1;
+  return 0;
+}
+
+extern "C" int bbpp_set_ff_resid(bbpp_ctx *ctx, int on) {
+  if (!ctx || (on != 0 && on != 1)) return BBPP_BAD_ARG;
+  ctx->ff_resid = on == 1;
+  drop_graphs(ctx);  // the replacement kernels are captured in the iteration graphs
   return 0;
 }
 

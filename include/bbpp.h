@@ -207,6 +207,9 @@ int bbpp_set_profiling(bbpp_ctx *ctx, int on);
  * iteration (the default where the TMA kernels take the grid), 0 = a search
  * kernel and an update kernel. */
 int bbpp_set_fused(bbpp_ctx *ctx, int on);
+/* The FP64 residuals of the reliable updates (FP64 x into the FP32 residual):
+ * 1 = float-float arithmetic on the FP32 pipe (the default), 0 = FP64. */
+int bbpp_set_ff_resid(bbpp_ctx *ctx, int on);
 
 /* ---- learned initial guess (no counterpart in the reference) ----
  * A 3-level 3D conv encoder-decoder (channels 16/32/64, 3x3x3 kernels, BF16

@@ -175,6 +175,29 @@ def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol, ir_mode):
     assert err < 1e4 * tol, err
 
 
+@pytest.mark.parametrize("name,n,bc", [("C3", 64, None), ("C2", 48, None), ("C1", 32, None), ("C3", 64, "nnn")])
+def test_ff_residual_matches_fp64(lib, orc, name, n, bc):
+    """Reliable-update residuals in float-float arithmetic against FP64: the
+    same PCG iterations within a few, both at the tolerance, and the
+    solutions as close as the tolerance allows."""
+    g, mask, rhs, _ = problems.make_problem(name, n=n)
+    if bc is not None:
+        g = problems.make_grid(n, bc)
+    s = bbpp.Solver(g)
+    out = {}
+    for ff in (True, False):
+        s.set_ff_resid(ff)
+        out[ff] = s.solve_host(rhs, mask, tol=1e-8, precision=bbpp.FP32_IR)
+    (xf, rf), (xd, rd) = out[True], out[False]
+    for rep in (rf, rd):
+        assert rep.status == bbpp.CONVERGED and rep.true_rel <= 1e-8 * 1.01
+    assert abs(rf.iters - rd.iters) <= max(3, rd.iters // 50)
+    assert rf.outer == rd.outer
+    if mask is None:
+        xf, xd = xf - xf.mean(), xd - xd.mean()
+    assert np.abs(xf - xd).max() <= 1e-5 * np.abs(xd).max()
+
+
 # grids the TMA kernels take (nx in 32 .. 256, a power of two), where the fused form exists
 @pytest.mark.parametrize("name,n,bc", [("C3", 64, None), ("C2", 128, None), ("C1", 32, None), ("C3", 64, "nnn"),
                                        ("C3", 64, "pnp")])
