@@ -752,7 +752,8 @@ __device__ __forceinline__ void resid_finish(DevState *st, const double (&tot)[3
 
 // ------------------------------------------------- float-float residual --
 // r = bscale rhs - L x for FP64 x and rhs into an FP32 r, evaluated in
-// float-float arithmetic on the FP32 pipe (GB300 issues FP64 at 1/64 of FP32).
+// float-float arithmetic on the FP32 pipe (GB300 issues FP64 at 1/64 of FP32);
+// an option beside the FP64 residual kernel, not its default replacement.
 // A value is an unevaluated sum hi + lo of two floats (about 48 bits); the
 // error-free transformations are Knuth's two-sum and the FMA two-product
 // (Dekker's product with a fused multiply-add), renormalised with

@@ -92,7 +92,7 @@ struct bbpp_ctx {
   bool rev_update = true;         // the update kernel walks the search kernel's planes in reverse
   bool l2hint = true;             // FP32 iteration: mask evict_last in L2, p / Ap / x evict_first
   bool fused = true;              // FP32 reliable-update solves: one fused kernel per iteration
-  bool ff_resid = true;           // FP64 x -> FP32 r residuals in float-float arithmetic
+  bool ff_resid = false;          // FP64 x -> FP32 r residuals in float-float arithmetic (else FP64)
   int inject = 0;                 // test hook of bbpp_debug_wait (see DevState::inject)
   long long wait_ns = 0;          // bound of device-side waits (0: one second)
 };

@@ -207,8 +207,9 @@ int bbpp_set_profiling(bbpp_ctx *ctx, int on);
  * iteration (the default where the TMA kernels take the grid), 0 = a search
  * kernel and an update kernel. */
 int bbpp_set_fused(bbpp_ctx *ctx, int on);
-/* The FP64 residuals of the reliable updates (FP64 x into the FP32 residual):
- * 1 = float-float arithmetic on the FP32 pipe (the default), 0 = FP64. */
+/* The outer residuals of the reliable updates (FP64 x into the FP32
+ * residual): 0 = FP64 arithmetic (the default), 1 = float-float arithmetic on
+ * the FP32 pipe (about 48 bits). */
 int bbpp_set_ff_resid(bbpp_ctx *ctx, int on);
 
 /* ---- learned initial guess (no counterpart in the reference) ----
