@@ -18,8 +18,11 @@
 //             thread), ring of three planes in shared memory while the CTA
 //             marches in z; Ap = L p and the (p, Ap) partial.
 //  k2_update  r -= alpha Ap, (r,r) and the wall correction of (r,z), 16-byte
-//             vector loads.
+//             vector loads; optionally in the reverse of the search kernel's
+//             plane order.
 //  k_resid_s  r = bscale rhs - L x (solid cells 0) with (r,z), (r,r), (rhs,rhs).
+//  k_resid_ff the same for FP64 x into FP32 r in float-float arithmetic (an
+//             option).
 #pragma once
 
 #include <type_traits>

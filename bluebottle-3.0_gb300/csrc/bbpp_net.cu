@@ -21,6 +21,9 @@
 //   OUT = D1 . w_head + b_head  (FP32)
 // Loss: mean over fluid cells of (OUT - (p* - p_prev) s_r / h^2)^2.
 // Padding is periodic in x and y and zero in z (the workloads' boundaries).
+// In a solve (bbpp_net_guess) the network runs, on large grids, on the
+// problem restricted by 2 and its correction is interpolated back.  The
+// forward convolution has a tcgen05 form (bbpp_conv_tc.cuh), off by default.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>

@@ -1,4 +1,7 @@
-// bbpp_tma.cu -- the FP32 search kernel with TMA-staged z-slabs.
+// bbpp_tma.cu -- the FP32 iteration kernels with TMA-staged z-slabs: the
+// search kernel of the two-kernel iteration (k1_tma), and the fused iteration
+// kernel (k1_fused, described where it is defined), which adds the previous
+// iteration's update to the same slab pipeline and L2 bulk prefetches.
 //
 // A CTA owns a slab of TY full x-rows (all nx cells of rows y0 .. y0+TY-1)
 // and marches through its z range.  For every plane one thread issues tensor
