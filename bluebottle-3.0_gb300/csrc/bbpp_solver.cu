@@ -417,7 +417,6 @@ static void launch_search_spmv(bbpp_ctx *ctx, const uint8_t *mask, const T *r, c
   // bytes/cell: read r, p_old (+ mask), write p_new, Ap; read and write x
   bbpp_rec_begin(ctx, sizeof(T) == 8 ? KK_SEARCH_SPMV : KK_SEARCH_SPMV_F32, 6.0 * sizeof(T) + (mask ? 1 : 0));
   const int prec = sizeof(T) == 8 ? 1 : 0;
-  cudaStream_t s = ctx->stream;
   if (sizeof(T) == 4 && bbpp_tma_search(ctx, mask, (const float *)r, (const float *)pold, (float *)pnew,
                                         (float *)Ap, (float *)x, st)) {
     // FP32 on a TMA-eligible grid: launched by bbpp_tma_search
