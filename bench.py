@@ -434,7 +434,11 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": H["ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32-inner/f64-refined" if headline == "ir" else "f64",
+        "vs_baseline": None,
+        # arithmetic of the headline method: FP32 PCG vectors with FP64 residuals, solution and dot
+        # accumulators (plus the BF16 network of the learned guess)
+        "dtype": {"ir": "f32-inner/f64-refined", "learned_ir": "f32-inner/f64-refined (+bf16 guess)"}.get(headline,
+                                                                                                       "f64"),
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "method": {"ir": "FP32 Jacobi PCG with FP64 reliable updates",
                                                      "learned_ir": "learned guess (C4 net, run on the grid "
