@@ -38,6 +38,7 @@
 #include "../../include/bbpp.h"
 #include "bbpp_conv.cuh"
 #include "bbpp_conv_tc.cuh"
+#include "bbpp_conv_tx.cuh"
 #include "bbpp_internal.h"
 
 using namespace bbnet;
@@ -73,7 +74,7 @@ cudaError_t conv_fwd_t(const ConvArgs &a, cudaStream_t s) {
 __device__ int g_tc_err;
 long long g_tc_launches = 0;  // tcgen05 convolutions launched by this process
 int g_tc_max_ctas = 0;        // > 0: cap on the persistent grid (tests: longer z marches per CTA)
-int g_tc_on = -1;             // -1: the environment decides (BBPP_CONV_TC=1 turns the kernel on)
+int g_tc_on = -1;             // -1: the environment decides (BBPP_CONV_TC, default 2)
 
 typedef CUresult (*TmEncode)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -167,17 +168,97 @@ cudaError_t conv_tc_t(const ConvArgs &a, cudaStream_t s) {
   return e;
 }
 
-// The tcgen05 kernel is off unless BBPP_CONV_TC=1 (or a test turns it on):
-// a tcgen05.mma of M = 128, K = 16 costs about 200 cycles whatever its N, and
-// these layers have N = 16 or 32 output channels per MMA, so the kernel runs
-// at ~150-250 TFLOP/s, no faster than the mma.sync kernel.
-bool conv_tc_enabled() {
+// the tx kernel: whole rows of 128 or 256 voxels, the three x-taps stacked in N
+bool tx_build(const TmKey &k, int rows, TxMaps *m) {
+  TmEncode fn = reinterpret_cast<TmEncode>(bbpp_tensor_map_encoder());
+  if (!fn) return false;
+  const cuuint64_t e = 2;
+  const cuuint64_t dim[5] = {(cuuint64_t)k.ldi, (cuuint64_t)k.nx, (cuuint64_t)k.ny, (cuuint64_t)k.nz,
+                             (cuuint64_t)k.nb};
+  const cuuint64_t str[4] = {k.ldi * e, k.nx * k.ldi * e, (cuuint64_t)k.ny * k.nx * k.ldi * e,
+                             (cuuint64_t)k.nz * k.ny * k.nx * k.ldi * e};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  const cuuint32_t box[5] = {8, (cuuint32_t)k.nx, (cuuint32_t)rows, 1, 1};
+  const cuuint32_t box1[5] = {8, (cuuint32_t)k.nx, 1, 1, 1};
+  if (fn(&m->rows, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(k.in), dim, str, box, es,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS ||
+      fn(&m->row, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(k.in), dim, str, box1, es,
+         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return false;
+  const cuuint64_t wdim[3] = {(cuuint64_t)k.cin, (cuuint64_t)k.cout, 27};
+  const cuuint64_t wstr[2] = {k.cin * e, (cuuint64_t)k.cout * k.cin * e};
+  const cuuint32_t wbox[3] = {8, (cuuint32_t)k.cout, 27};
+  return fn(&m->w, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(k.w), wdim, wstr, wbox, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool tx_maps(const TmKey &k, int rows, TxMaps *out) {
+  static std::vector<std::pair<TmKey, TxMaps>> cache;
+  for (const auto &c : cache)
+    if (c.first == k) {
+      *out = c.second;
+      return true;
+    }
+  TxMaps m;
+  if (!tx_build(k, rows, &m)) return false;
+  if (cache.size() >= 32) cache.erase(cache.begin());
+  cache.emplace_back(k, m);
+  *out = m;
+  return true;
+}
+
+template <int CIN, int COUT, int NXB>
+cudaError_t conv_tx_t(const ConvArgs &a, cudaStream_t s) {
+  // at least half an SM's shared memory: one CTA per SM (each holds all of tensor memory)
+  constexpr int smem = std::max(tx_smem<CIN, COUT, NXB>(), 116 * 1024);
+  constexpr int TYR = tx_tyr<COUT, NXB>();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static unsigned long long attr = 0;  // per device
+  if (dev < 64 && !(attr & (1ull << dev))) {
+    cudaError_t e = cudaFuncSetAttribute(k_conv3_tx<CIN, COUT, NXB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem);
+    if (e != cudaSuccess) return e;
+    attr |= 1ull << dev;
+  }
+  TmKey key{a.in, a.w, a.ldi, a.nx, a.ny, a.nz, a.nb, CIN, COUT};
+  TxMaps maps;
+  if (!tx_maps(key, TYR + 2, &maps)) return cudaErrorNotSupported;  // the caller falls back
+  TxGeo g;
+  g.nyb = (a.ny + TYR - 1) / TYR;
+  g.units = (long long)a.nb * g.nyb * a.nz;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int cap = std::max(sms, 1);
+  if (g_tc_max_ctas > 0) cap = std::min(cap, g_tc_max_ctas);
+  const int grid = (int)std::min<long long>(cap, g.units);
+  int *err = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void **)&err, g_tc_err);
+  if (e != cudaSuccess) return e;
+  k_conv3_tx<CIN, COUT, NXB><<<grid, TX_THREADS, smem, s>>>(a, maps, g, err);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) g_tc_launches++;
+  return e;
+}
+
+// Forward convolution kernel: 0 = mma.sync, 1 = tcgen05 with x-shifted A tiles
+// in tensor memory (k_conv3_tm), 2 = tcgen05 with the x-taps stacked in N
+// (k_conv3_tx, the default; BBPP_CONV_TC=0 or 1 selects the others).  A
+// tcgen05.mma of M = 128, K = 16 costs about the same whatever its N, so
+// k_conv3_tm, with N = 16 or 32 output channels, is no faster than mma.sync;
+// k_conv3_tx, with N = 48 or 96, is 1.6-2.3 times faster on these layers.
+int conv_tc_mode() {
   if (g_tc_on < 0) {
     const char *v = getenv("BBPP_CONV_TC");
-    return v && v[0] == '1';
+    return (v && (v[0] == '0' || v[0] == '1')) ? v[0] - '0' : 2;
   }
-  return g_tc_on == 1;
+  return g_tc_on;
 }
+
+bool conv_tc_enabled() { return conv_tc_mode() != 0; }
 
 // the tcgen05 kernel takes 128-voxel x blocks, 16-byte aligned channel runs and
 // tensor maps (a driver with cuTensorMapEncodeTiled)
@@ -198,11 +279,23 @@ int conv_tc_failed() {
   return v;
 }
 
+// rows of 128 voxels (and of 256 where COUT = 16); other widths fall back
+template <int CIN, int COUT>
+cudaError_t conv_tx_rows(const ConvArgs &a, cudaStream_t s) {
+  if (a.nx == 128) return conv_tx_t<CIN, COUT, 1>(a, s);
+  if constexpr (COUT == 16) {
+    if (a.nx == 256) return conv_tx_t<CIN, COUT, 2>(a, s);
+  }
+  return cudaErrorNotSupported;
+}
+
 cudaError_t conv_fwd(int cin, int cout, const ConvArgs &a, cudaStream_t s) {
-#define TCASE(CI, CO)                                     \
-  if (cin == CI && cout == CO && conv_tc_fits(a)) {         \
-    const cudaError_t e_ = conv_tc_t<CI, CO>(a, s);         \
-    if (e_ != cudaErrorNotSupported) return e_;             \
+#define TCASE(CI, CO)                                                                     \
+  if (cin == CI && cout == CO && conv_tc_fits(a)) {                                         \
+    cudaError_t e_ = cudaErrorNotSupported;                                                 \
+    if (conv_tc_mode() == 2) e_ = conv_tx_rows<CI, CO>(a, s);                               \
+    else e_ = conv_tc_t<CI, CO>(a, s);                                                      \
+    if (e_ != cudaErrorNotSupported) return e_;                                             \
   }
   TCASE(16, 16) TCASE(16, 32) TCASE(96, 32) TCASE(48, 16) TCASE(32, 16)
 #undef TCASE
@@ -1223,10 +1316,10 @@ extern "C" int bbpp_conv3(int cin, int cout, const void *in, int ldi, int ci_off
 // Number of convolutions that ran on the tcgen05 kernel in this process.
 extern "C" long long bbpp_conv3_tc_launches(void) { return g_tc_launches; }
 
-// Kernel choice: enable (1) or disable (0) the tcgen05 kernel, or (-1) leave
-// the choice to BBPP_CONV_TC; and cap its persistent grid (0: one CTA per SM).
+// Kernel choice: mma.sync (0), k_conv3_tm (1), k_conv3_tx (2), or (-1) leave the
+// choice to BBPP_CONV_TC; and cap the persistent grid (0: one CTA per SM).
 extern "C" int bbpp_conv3_tc_config(int enable, int max_ctas) {
-  if (enable < -1 || enable > 1 || max_ctas < 0) return BBPP_BAD_ARG;
+  if (enable < -1 || enable > 2 || max_ctas < 0) return BBPP_BAD_ARG;
   g_tc_on = enable;
   g_tc_max_ctas = max_ctas;
   return 0;

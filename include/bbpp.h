@@ -250,14 +250,16 @@ int bbpp_conv3(int cin, int cout, const void *in, int ldi, int ci_off, const voi
 int bbpp_conv3_wgrad(int cin, int cout, const void *in, int ldi, int ci_off, const void *g, int ldg, float *dW,
                      int nx, int ny, int nz, int nb, int px, int py, int pz);
 int bbpp_conv3_wflip(int cin, int cout, const void *w, void *wt);
-/* Convolutions run so far on the tcgen05 (tensor-memory) kernel.  When it is
- * enabled, forward layers with 16 or 32 outputs on 128-voxel x blocks take
- * it; the others, and all layers when it is off (the default), take the
- * mma.sync kernel. */
+/* Convolutions run so far on a tcgen05 (tensor-memory) kernel.  With the
+ * default choice, forward layers with 16 or 32 outputs on rows of 128 voxels
+ * (or 16 outputs on rows of 256) take it; the others take the mma.sync kernel. */
 long long bbpp_conv3_tc_launches(void);
-/* Enable (1) / disable (0) the tcgen05 kernel, or (-1) leave the choice to
- * the environment (BBPP_CONV_TC=1 enables it); cap its persistent grid at
- * max_ctas CTAs (0: one per SM). */
+/* Choose the forward convolution kernel: 0 mma.sync; 1 tcgen05 with x-shifted
+ * A tiles in tensor memory; 2 tcgen05 with the three x-taps stacked in N
+ * (the default: rows of 128 voxels, or 256 with 16 output channels; other
+ * widths take mma.sync); -1 leaves the choice to the environment
+ * (BBPP_CONV_TC=0, 1 or 2; 2 when unset).
+ * Caps the persistent grid at max_ctas CTAs (0: one per SM). */
 int bbpp_conv3_tc_config(int enable, int max_ctas);
 
 /* Ranq1 generator (src/rng.c:25-107), for reproducible synthetic inputs. */

@@ -46,11 +46,12 @@ CONVS = [(16, 16), (16, 32), (32, 64), (96, 32), (48, 16)]
 
 
 @pytest.mark.parametrize("cin,cout", CONVS)
-# rows of 128 voxels take the tcgen05 kernel (16 or 32 output channels) when it
-# is enabled, the others the mma.sync kernel
+# rows of 128 voxels take a tcgen05 kernel (16 or 32 output channels; 256 too
+# for k_conv3_tm, and for k_conv3_tx with 16), the others the mma.sync kernel
 @pytest.mark.parametrize("dims,pads", [((20, 12, 6), (1, 1, 0)), ((16, 8, 4), (0, 0, 0)), ((33, 9, 3), (1, 0, 1)),
                                        ((128, 5, 3), (1, 1, 0)), ((256, 2, 5), (0, 1, 1))])
-def test_conv3_forward_dgrad_wgrad(bbpp_lib, cin, cout, dims, pads):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_conv3_forward_dgrad_wgrad(bbpp_lib, cin, cout, dims, pads, mode):
     L = learned._sig()
     nx, ny, nz = dims
     px, py, pz = pads
@@ -63,14 +64,15 @@ def test_conv3_forward_dgrad_wgrad(bbpp_lib, cin, cout, dims, pads):
     db = bbpp.DeviceArray.from_host(bias)
     dy = bbpp.DeviceArray((nb, nz, ny, nx, cout), np.uint16)
     tc0 = L.bbpp_conv3_tc_launches()
-    assert L.bbpp_conv3_tc_config(1, 0) == 0
+    assert L.bbpp_conv3_tc_config(mode, 0) == 0
     try:
         assert L.bbpp_conv3(cin, cout, dx.ptr, cin, 0, dw.ptr, db.ptr, dy.ptr, cout, 0, nx, ny, nz, nb, px, py, pz,
                             0) == 0
     finally:
         L.bbpp_conv3_tc_config(-1, 0)
-    # with the tcgen05 kernel enabled, the shapes it takes ran on it
-    assert L.bbpp_conv3_tc_launches() - tc0 == (1 if nx % 128 == 0 and cout in (16, 32) else 0)
+    # the shapes a tcgen05 kernel takes ran on it
+    rows = nx % 128 == 0 if mode == 1 else (nx == 128 or (nx == 256 and cout == 16))
+    assert L.bbpp_conv3_tc_launches() - tc0 == (1 if rows and cout in (16, 32) else 0)
     y = NO.bits_f32(dy.download())
     xt, wt = torch_conv(x, w, px, py, pz)
     xt.requires_grad_(True)
@@ -105,10 +107,13 @@ TC_CONVS = [(16, 16), (16, 32), (96, 32), (48, 16), (32, 16)]
 @pytest.mark.parametrize("dims,pads,nb", [((256, 8, 10), (1, 1, 0), 1), ((128, 6, 12), (1, 1, 0), 2),
                                           ((256, 5, 9), (0, 1, 1), 1)])
 @pytest.mark.parametrize("ctas", [1, 5])
-def test_conv3_tc_marching(bbpp_lib, cin, cout, dims, pads, nb, ctas):
-    """The tcgen05 kernel with few CTAs, so each marches through many planes
+@pytest.mark.parametrize("mode", [1, 2])
+def test_conv3_tc_marching(bbpp_lib, cin, cout, dims, pads, nb, ctas, mode):
+    """The tcgen05 kernels with few CTAs, so each marches through many planes
     and tiles (accumulator ring reuse, segment changes, one- and two-sided
-    periodic x wrap), writing into a channel window of a wider output."""
+    periodic x wrap), writing into a channel window of a wider output.  Mode 1
+    is k_conv3_tm (x-shifted A tiles in tensor memory), mode 2 k_conv3_tx (the
+    x-taps stacked in N; rows of 128 voxels, or 256 with 16 output channels)."""
     L = learned._sig()
     nx, ny, nz = dims
     px, py, pz = pads
@@ -122,13 +127,14 @@ def test_conv3_tc_marching(bbpp_lib, cin, cout, dims, pads, nb, ctas):
     dy = bbpp.DeviceArray((nb, nz, ny, nx, ldo), np.uint16)
     dy.zero()
     tc0 = L.bbpp_conv3_tc_launches()
-    assert L.bbpp_conv3_tc_config(1, ctas) == 0
+    assert L.bbpp_conv3_tc_config(mode, ctas) == 0
     try:
         assert L.bbpp_conv3(cin, cout, dx.ptr, cin, 0, dw.ptr, db.ptr, dy.ptr, ldo, co_off, nx, ny, nz, nb, px, py,
                             pz, 1) == 0
     finally:
         L.bbpp_conv3_tc_config(-1, 0)
-    assert L.bbpp_conv3_tc_launches() - tc0 == 1
+    taken = mode == 1 or nx == 128 or (nx == 256 and cout == 16)
+    assert L.bbpp_conv3_tc_launches() - tc0 == (1 if taken else 0)
     y = NO.bits_f32(dy.download())
     xt, wt = torch_conv(x, w, px, py, pz)
     yref = torch.relu(conv_ref(xt, wt, px, py, pz) + torch.as_tensor(bias).view(1, -1, 1, 1, 1))
