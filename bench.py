@@ -473,6 +473,68 @@ def run_ours(args):
         print(json.dumps(line))
 
 
+# forward layers of the learned guess's network: (cin, cout, n, ldi, ldo, co_off),
+# n^3 volume, input channel stride ldi, output written at channel co_off of ldo
+CONV_LAYERS = [(16, 16, 128, 16, 48, 32), (48, 16, 128, 48, 16, 0), (16, 16, 256, 16, 48, 32),
+               (48, 16, 256, 48, 16, 0), (16, 32, 128, 16, 96, 64), (96, 32, 128, 96, 32, 0)]
+CONV_KERNELS = {0: "mma_sync", 1: "tcgen05_tm", 2: "tcgen05_tx"}
+
+
+def conv_layers(args):
+    """Per-layer timing of the forward 3x3x3 convolution on each kernel
+    (CUDA events on the launching stream, best of --steps after --warmup),
+    one JSON line per layer: not the headline, the evidence for the choice of
+    convolution kernel."""
+    import numpy as np
+    import torch
+    import bbpp
+    from bbpp import learned
+    L = learned._sig()
+    layers = CONV_LAYERS
+    if args.conv_layers:
+        want = [tuple(int(v) for v in spec.split(",")) for spec in args.conv_layers]
+        layers = [c for c in CONV_LAYERS if c[:3] in want]
+    modes = [int(m) for m in args.conv_modes.split(",")]
+    for cin, cout, n, ldi, ldo, co in layers:
+        rng = np.random.default_rng(cin + cout + n)
+        x32 = rng.normal(size=(1, n, n, n, ldi)).astype(np.float32)
+        x = (x32.view(np.uint32) >> 16).astype(np.uint16)  # BF16 bits (truncated)
+        w = ((rng.normal(size=(27, cout, cin)) * 0.1).astype(np.float32).view(np.uint32) >> 16).astype(np.uint16)
+        bias = rng.normal(size=cout).astype(np.float32)
+        dx, dw, db = bbpp.DeviceArray.from_host(x), bbpp.DeviceArray.from_host(w), bbpp.DeviceArray.from_host(bias)
+        dy = bbpp.DeviceArray((1, n, n, n, ldo), np.uint16)
+        flop = 2.0 * n ** 3 * 27 * cin * cout
+        rec = {"conv_layer": "%d->%d" % (cin, cout), "n": n, "periodic": "x,y", "ms": {}, "tflops": {},
+               "tcgen05_launches": {}}
+
+        def call():
+            rc = L.bbpp_conv3(cin, cout, dx.ptr, ldi, 0, dw.ptr, db.ptr, dy.ptr, ldo, co, n, n, n, 1, 1, 1, 0, 1)
+            if rc != 0:
+                raise RuntimeError("bbpp_conv3 returned %d" % rc)
+
+        for mode in modes:
+            assert L.bbpp_conv3_tc_config(mode, 0) == 0
+            tc0 = L.bbpp_conv3_tc_launches()
+            for _ in range(args.warmup):
+                call()
+            best = None
+            for _ in range(args.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record()  # the default stream, which bbpp_conv3 launches on
+                call()
+                e1.record()
+                torch.cuda.synchronize()
+                t = e0.elapsed_time(e1)
+                best = t if best is None else min(best, t)
+            name = CONV_KERNELS[mode]
+            rec["ms"][name] = best
+            rec["tflops"][name] = flop / (best * 1e-3) / 1e12
+            rec["tcgen05_launches"][name] = L.bbpp_conv3_tc_launches() - tc0
+        L.bbpp_conv3_tc_config(-1, 0)
+        print(json.dumps(rec), flush=True)
+
+
 def main():
     faulthandler.enable()  # a crash in native code prints the Python stack
     ap = argparse.ArgumentParser()
@@ -490,9 +552,14 @@ def main():
                     help="run only warm-up + steps solves of one method (profiler runs)")
     ap.add_argument("--ref-iters", type=int, default=0,
                     help="iterations of a full solve for the reference arm (0: the measured C3 count)")
+    ap.add_argument("--conv-layers", nargs="*", default=None, metavar="CIN,COUT,N",
+                    help="time the forward convolution layers (all, or the ones named) on each kernel instead")
+    ap.add_argument("--conv-modes", default="0,1,2", help="convolution kernels to time (0 mma.sync, 1 tm, 2 tx)")
     args = ap.parse_args()
     args.steps = max(1, args.steps)
-    if args.impl == "reference":
+    if args.conv_layers is not None:
+        conv_layers(args)
+    elif args.impl == "reference":
         if args.ref_iters <= 0:
             args.ref_iters = C3_FP64_ITERS or 1000
         run_reference(args)
