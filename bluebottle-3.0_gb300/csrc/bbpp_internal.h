@@ -74,7 +74,8 @@ struct bbpp_ctx {
   double *r = nullptr, *p[2] = {nullptr, nullptr}, *Ap = nullptr;
   double *hbuf_rhs = nullptr, *hbuf_x = nullptr;
   uint8_t *hbuf_mask = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaStream_t copy_stream = nullptr;  // the host-buffer solve's copy of x, beside its residual check
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_copy = nullptr;
   std::vector<GraphCache> graphs;
   bool profiling = false;
   std::vector<KEv> *rec = nullptr;   // when set, launches record events here
