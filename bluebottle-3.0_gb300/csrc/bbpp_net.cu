@@ -649,12 +649,46 @@ __global__ void k_guess_out(const float *__restrict__ out, const double *__restr
     x[i] = (mask && mask[i]) ? 0.0 : (prev ? prev[i] : 0.0) + (double)out[i] * sr;
 }
 
+// binary64 -> binary32 by truncating the significand (round toward zero): the
+// exponent is rebiased (1023 -> 127) and the 52-bit fraction cut to its top 23
+// bits.  Magnitudes below the binary32 normal range become a signed zero,
+// finite magnitudes above it the largest finite binary32; infinities and NaNs
+// stay so.  Integer operations only: a cvt runs on the FP64 pipe, which on
+// this part has 1/64 of the FP32 rate, and the grid kernels of the guess
+// convert several values per cell.
+__device__ __forceinline__ float narrow_rz(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned int hi = (unsigned int)(b >> 32);
+  const unsigned int sign = hi & 0x80000000u;
+  const int e64 = (int)((hi >> 20) & 0x7ffu);
+  const unsigned int frac = (unsigned int)(b >> 29) & 0x7fffffu;
+  if (e64 == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (frac ? 0x400000u : 0u));
+  const int e = e64 - 1023 + 127;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7f7fffffu);
+  return __uint_as_float(sign | ((unsigned int)e << 23) | frac);
+}
+
+// binary32 -> binary64, exact for normal numbers and zeros (exponent rebiased,
+// fraction widened); binary32 subnormals become a signed zero, infinities and
+// NaNs stay so.  Integer operations only, as narrow_rz.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned int e32 = (u >> 23) & 0xffu;
+  const unsigned long long frac = (unsigned long long)(u & 0x7fffffu) << 29;
+  if (e32 == 0) return __longlong_as_double((long long)sign);
+  if (e32 == 0xffu) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | frac));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e32 - 127u + 1023u) << 52) | frac));
+}
+
 // The warm start's residual r = rhs - (-A) p_prev, restricted by 2 in the same
 // pass (cell-centred: the means of the 2x2x2 children), with p_prev's means
 // and the coarse solid cells (at least 4 solid children).  The residual is
 // formed as in the residual kernel (k_resid: neighbours of or across solid
-// cells count 0, walls through the class diagonal) but in FP32 arithmetic: it
-// only feeds the BF16 network.  prev == NULL: r = rhs, p_prev = 0.
+// cells count 0, walls through the class diagonal) but in FP32 arithmetic, on
+// inputs narrowed by truncation (narrow_rz): it only feeds the BF16 network.
+// prev == NULL: r = rhs, p_prev = 0.
 __global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, const double *__restrict__ rhs,
                                                          const double *__restrict__ prev,
                                                          const uint8_t *__restrict__ mask, double *__restrict__ rc,
@@ -674,7 +708,7 @@ __global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, cons
     if (gx < 0 || gy < 0 || gz < 0) return 0.f;
     const unsigned int c = (unsigned)gx + (unsigned)nx * ((unsigned)gy + (unsigned)ny * (unsigned)gz);
     if (mask) solid = mask[c] != 0;
-    return (float)prev[c];
+    return narrow_rz(prev[c]);
   };
   for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < nc; e += gridDim.x * 256u) {
     const unsigned int i = e % cxn, t = e / cxn, j = t % cyn, k = t / cyn;
@@ -685,9 +719,9 @@ __global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, cons
       const int x = 2 * (int)i + (ch & 1), y = 2 * (int)j + ((ch >> 1) & 1), z = 2 * (int)k + (ch >> 2);
       const unsigned int c = (unsigned)x + (unsigned)nx * ((unsigned)y + (unsigned)ny * (unsigned)z);
       const bool ms = mask && mask[c] != 0;
-      float r = (float)rhs[c];
+      float r = narrow_rz(rhs[c]);
       if (prev) {
-        const float pcv = (float)prev[c];
+        const float pcv = narrow_rz(prev[c]);
         bool s0, s1, s2, s3, s4, s5;
         float pe = nb(x + 1, y, z, s0), pw = nb(x - 1, y, z, s1), pn = nb(x, y + 1, z, s2), ps = nb(x, y - 1, z, s3);
         float pt = nb(x, y, z + 1, s4), pb = nb(x, y, z - 1, s5);
@@ -717,11 +751,12 @@ __global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, cons
   }
 }
 
-// the coarse correction p0c - pc (0 on coarse solid cells), in place of p0c
-__global__ void k_corr2(double *__restrict__ p0c, const double *__restrict__ pc, const uint8_t *__restrict__ mc,
-                        unsigned int nc) {
+// the coarse correction p0c - pc (0 on coarse solid cells) in FP32: the
+// prolongation interpolates it in FP32
+__global__ void k_corr2(float *__restrict__ corr, const double *__restrict__ p0c, const double *__restrict__ pc,
+                        const uint8_t *__restrict__ mc, unsigned int nc) {
   for (unsigned int e = blockIdx.x * 256u + threadIdx.x; e < nc; e += gridDim.x * 256u)
-    p0c[e] = mc[e] ? 0.0 : p0c[e] - pc[e];
+    corr[e] = mc[e] ? 0.f : (float)(p0c[e] - pc[e]);
 }
 
 // one axis of the cell-centred trilinear prolongation by 2: fine cell a lies
@@ -746,9 +781,10 @@ __device__ __forceinline__ void prolong_axis(int a, int n, int periodic, int &lo
   }
 }
 
-// x = p_prev + the trilinear interpolation of the coarse correction; fine
-// solid cells 0, as the guess on the grid itself
-__global__ void __launch_bounds__(256) k_prolong2(const double *__restrict__ corr, const double *__restrict__ prev,
+// x = p_prev + the trilinear interpolation of the coarse correction (FP32,
+// widened exactly before the FP64 add); fine solid cells 0, as the guess on
+// the grid itself
+__global__ void __launch_bounds__(256) k_prolong2(const float *__restrict__ corr, const double *__restrict__ prev,
                                                   const uint8_t *__restrict__ mask, int nx, int ny, int nz, int px,
                                                   int py, int pz, double *__restrict__ x) {
   const int cxn = nx >> 1, cyn = ny >> 1, czn = nz >> 1;
@@ -768,12 +804,12 @@ __global__ void __launch_bounds__(256) k_prolong2(const double *__restrict__ cor
     prolong_axis(k, czn, pz, zl, zh, wz);
     const unsigned int r00 = ((unsigned)zl * cyn + yl) * cxn, r01 = ((unsigned)zl * cyn + yh) * cxn;
     const unsigned int r10 = ((unsigned)zh * cyn + yl) * cxn, r11 = ((unsigned)zh * cyn + yh) * cxn;
-    const float a00 = (1.f - wx) * (float)corr[r00 + xl] + wx * (float)corr[r00 + xh];
-    const float a01 = (1.f - wx) * (float)corr[r01 + xl] + wx * (float)corr[r01 + xh];
-    const float a10 = (1.f - wx) * (float)corr[r10 + xl] + wx * (float)corr[r10 + xh];
-    const float a11 = (1.f - wx) * (float)corr[r11 + xl] + wx * (float)corr[r11 + xh];
+    const float a00 = (1.f - wx) * corr[r00 + xl] + wx * corr[r00 + xh];
+    const float a01 = (1.f - wx) * corr[r01 + xl] + wx * corr[r01 + xh];
+    const float a10 = (1.f - wx) * corr[r10 + xl] + wx * corr[r10 + xh];
+    const float a11 = (1.f - wx) * corr[r11 + xl] + wx * corr[r11 + xh];
     const float v = (1.f - wz) * ((1.f - wy) * a00 + wy * a01) + wz * ((1.f - wy) * a10 + wy * a11);
-    x[f] = (prev ? prev[f] : 0.0) + (double)v;
+    x[f] = prev ? prev[f] + widen(v) : widen(v);
   }
 }
 
@@ -1349,6 +1385,7 @@ struct NetWork {
   double *prev0 = nullptr;  // zero "previous pressure" when none is given
   // the problem restricted by 2: r, p_prev, the network's p0; the solid cells
   double *rc = nullptr, *pc = nullptr, *p0c = nullptr;
+  float *corr = nullptr;  // p0c - pc in FP32 (0 on coarse solid cells)
   uint8_t *mc = nullptr;
   long long ncap = 0;
 };
@@ -1377,13 +1414,16 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
       cudaFree(w->pc);
       cudaFree(w->p0c);
       cudaFree(w->mc);
+      cudaFree(w->corr);
       w->rc = w->pc = w->p0c = nullptr;
+      w->corr = nullptr;
       w->mc = nullptr;
       w->ncap = 0;
       NCK(cudaMalloc(&w->rc, nc * sizeof(double)));
       NCK(cudaMalloc(&w->pc, nc * sizeof(double)));
       NCK(cudaMalloc(&w->p0c, nc * sizeof(double)));
       NCK(cudaMalloc(&w->mc, nc));
+      NCK(cudaMalloc(&w->corr, nc * sizeof(float)));
       w->ncap = nc;
     }
   }
@@ -1412,8 +1452,8 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
     }
     if (rc == 0) rc = bbpp_net_infer(n, nx / 2, ny / 2, nz / 2, 4.0 * h2, w->rc, w->pc, mask ? w->mc : nullptr, w->p0c);
     if (rc == 0) {
-      k_corr2<<<nblocks(nc), 256, 0, ctx->stream>>>(w->p0c, w->pc, w->mc, (unsigned)nc);
-      k_prolong2<<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->p0c, prev, mask, nx, ny, nz, ctx->G.px, ctx->G.py,
+      k_corr2<<<nblocks(nc), 256, 0, ctx->stream>>>(w->corr, w->p0c, w->pc, w->mc, (unsigned)nc);
+      k_prolong2<<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->corr, prev, mask, nx, ny, nz, ctx->G.px, ctx->G.py,
                                                               ctx->G.pz, x);
       if (cudaGetLastError() != cudaSuccess) rc = BBPP_CUDA_ERROR;
     }
@@ -1443,6 +1483,7 @@ void bbpp_net_ctx_free(bbpp_ctx *ctx) {
     cudaFree(ctx->net->pc);
     cudaFree(ctx->net->p0c);
     cudaFree(ctx->net->mc);
+    cudaFree(ctx->net->corr);
     delete ctx->net;
     ctx->net = nullptr;
   }
