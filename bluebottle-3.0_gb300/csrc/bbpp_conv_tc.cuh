@@ -1,6 +1,9 @@
 // bbpp_conv_tc.cuh -- forward 3x3x3 convolution on the 5th-generation tensor
 // cores: tcgen05.mma with the A operand in tensor memory, FP32 accumulators in
-// tensor memory, operands staged by TMA.
+// tensor memory, operands staged by TMA.  Selected by BBPP_CONV_TC=1 (or
+// bbpp_conv3_tc_config(1, ...)); the default forward kernel is k_conv3_tx
+// (bbpp_conv_tx.cuh), which needs a third of the MMAs.  The shared helpers
+// (descriptors, bounded waits, TMA, tensor-memory loads) are used by both.
 //
 // Implicit GEMM, input-row stationary.  A CTA works on 128-voxel x blocks of
 // TYR output rows and marches in z.  Per input plane and 16-channel chunk the

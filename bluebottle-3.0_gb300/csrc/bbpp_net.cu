@@ -22,8 +22,10 @@
 // Loss: mean over fluid cells of (OUT - (p* - p_prev) s_r / h^2)^2.
 // Padding is periodic in x and y and zero in z (the workloads' boundaries).
 // In a solve (bbpp_net_guess) the network runs, on large grids, on the
-// problem restricted by 2 and its correction is interpolated back.  The
-// forward convolution has a tcgen05 form (bbpp_conv_tc.cuh), off by default.
+// problem restricted by 2 and its correction is interpolated back.  Forward
+// convolutions on rows of 128 voxels (or 256 with 16 outputs) run on tcgen05
+// with the x-taps stacked in N (bbpp_conv_tx.cuh); the others, the data
+// gradients and the weight gradients on mma.sync (bbpp_conv.cuh).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
