@@ -67,6 +67,25 @@ def test_solid_rows_identity_like(orc):
     assert np.allclose(F, F.T, atol=1e-9 * np.abs(F).max())
 
 
+@pytest.mark.parametrize("bc,seed", [((P,) * 6, 1), ((P, P, P, P, N, N), 2), ((N,) * 6, 3), ((P, P, N, N, P, P), 4)])
+def test_fluid_block_positive_semidefinite(orc, bc, seed):
+    """(-A) restricted to the fluid cells is symmetric positive semi-definite for
+    any solid set, including solids on the periodic seams and the walls; its
+    solid rows stay decoupled.  Positive semi-definiteness on the fluid subspace
+    is what the PCG relies on."""
+    g = orc.grid(6, 5, 4, bc=bc)
+    rng = np.random.default_rng(seed)
+    mask = (rng.random((4, 5, 6)) < 0.25).astype(np.uint8)
+    mask[0, 0, :] = 1  # a row of solids along a seam / wall
+    A = dense(orc, g, mask)
+    m = mask.ravel().astype(bool)
+    F = A[np.ix_(~m, ~m)]
+    assert np.allclose(F, F.T, rtol=0, atol=1e-9 * np.abs(F).max())
+    w = np.linalg.eigvalsh(0.5 * (F + F.T))
+    assert w.min() > -1e-9 * w.max()
+    assert np.abs(A[np.ix_(~m, m)]).max() == 0 and np.abs(A[np.ix_(m, ~m)]).max() == 0
+
+
 def test_invm_matches_diag(orc):
     g = orc.grid(5, 4, 6, bc=(P, P, N, N, N, N))
     A = dense(orc, g)
