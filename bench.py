@@ -28,10 +28,6 @@ METRIC = "256³ Poisson time-to-1e-8 residual: learned+mixed vs plain FP64 PCG, 
 UNIT = "solves/s"
 WORKLOAD = ("C3: 256^3 cells, periodic x/y + Neumann z, 1000 spheres r=6 cells, k^-11/3 RHS (step 1 of an OU "
             "sequence), tol 1e-8 (true rel.)")
-# Plain FP64 PCG iterations of the C3 workload to 1e-8 (seed 3), measured by
-# the CUDA path and equal to the oracle's count; used to scale the bounded CPU
-# sample of the reference arm to a full solve.
-C3_FP64_ITERS = 604
 # DRAM bytes (read + write) per launch of the dominant kernels on this workload,
 # from one ncu capture each (--set full, two launches of a 256^3 solve; the
 # summaries sit with the other profiles): kernel kind -> bytes
@@ -184,11 +180,18 @@ def reference_gpu(g, mask, rhs, tol, args):
             return {"unavailable": "reference solve status %d" % rc}
         times.append(ms)
         its.append(it)
+    # the same solver run tight (pp_residual 2e-15: a true relative residual
+    # near 1e-12 at this size), the FP64 solution the methods are also compared with
+    phi, it_t, res_t, ms_t, rc_t = ref.solve(rhs, 2e-15)
     ref.close()
     ms = float(np.mean(times[1:]))
-    return {"value": 1000.0 / ms, "unit": UNIT, "ms_per_solve": ms, "iters": its[-1],
-            "stop": "(r,z) <= tol^2 (b,b), the reference's rule",
-            "kind": "reference CUDA kernels (src/solver_kernel.cu, unmodified) on this GPU, one rank"}
+    out = {"value": 1000.0 / ms, "unit": UNIT, "ms_per_solve": ms, "iters": its[-1],
+           "stop": "(r,z) <= tol^2 (b,b), the reference's rule",
+           "kind": "reference CUDA kernels (src/solver_kernel.cu, unmodified) on this GPU, one rank"}
+    if rc_t == 0:
+        out["tight"] = {"pp_residual": 2e-15, "iters": it_t}
+        out["_phi"] = phi
+    return out
 
 
 def profiler_api():
@@ -202,56 +205,78 @@ def profiler_api():
     return lambda on: (cu.cuProfilerStart() if on else cu.cuProfilerStop())
 
 
-def cpu_sample(g, rhs, mask, iters_full, threads):
-    """Time the oracle PCG on the full-size workload for a bounded number of
-    iterations and scale to a full solve: t = t_setup + t_iter * iters_full."""
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:  # noqa: BLE001
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def oracle_mod():
+    """The CPU oracle (pyoracle) and its input generator (pyproblems)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    og = pyoracle.from_tuple(g.as_tuple())
-    pyoracle.lib()
-    k1, k2 = 1, 6
+    import pyproblems
+    return pyoracle, pyproblems
+
+
+def oracle_solve(og, rhs, mask, tol, x0=None):
+    """One complete plain FP64 Jacobi-PCG solve by the oracle (OpenMP over the
+    host cores) to a true relative residual of tol: (seconds, x, result)."""
+    pyoracle, _ = oracle_mod()
     t0 = time.perf_counter()
-    pyoracle.pcg(og, rhs, mask, tol=1e-30, max_iter=k1 - 1)
-    t1 = time.perf_counter()
-    pyoracle.pcg(og, rhs, mask, tol=1e-30, max_iter=k2 - 1)
-    t2 = time.perf_counter()
-    t_iter = ((t2 - t1) - (t1 - t0)) / (k2 - k1)
-    t_setup = max((t1 - t0) - k1 * t_iter, 0.0)
-    t_solve = t_setup + t_iter * iters_full
-    return 1.0 / t_solve, {"t_iter_s": t_iter, "t_setup_s": t_setup, "iters_full": iters_full,
-                           "sampled_iters": k1 + k2, "wall_s": t2 - t0}
+    x, res = pyoracle.pcg(og, rhs, mask, tol=tol, x0=x0)
+    t = time.perf_counter() - t0
+    if res["status"] != 0:
+        raise RuntimeError("oracle solve did not converge: %s" % res)
+    return t, x, res
+
+
+def pyoracle_true_rel(g, rhs, x, mask):
+    """||rhs - (-A)x|| / ||rhs|| by the oracle."""
+    pyoracle, _ = oracle_mod()
+    return float(pyoracle.true_rel(pyoracle.from_tuple(g.as_tuple()), rhs, x, mask))
 
 
 def run_reference(args):
-    """CPU arm: the reference's algorithm in plain C (the oracle) on host cores."""
-    rank, world, barrier, vmax = dist_init(args.gpus)
+    """CPU arm: the reference's algorithm in plain C (the oracle, OpenMP on all
+    host cores).  Every step is one complete solve of the C3 workload to the
+    same 1e-8 true relative residual; the inputs come from the oracle's own
+    generator, so this arm loads no library of the solver."""
+    rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    import numpy as np
-    import bbpp
-    from bbpp import problems
-    g, cents, radii, c = make_c3()
-    mask = problems.sphere_mask_host(g, cents, radii)
-    seq = problems.OUSequence(g.shape, c["seed"], mask)
-    seq.field()
-    rhs = seq.step()  # the same right-hand side as the GPU arm
     threads = os.cpu_count() or 1
-    iters = args.ref_iters
-    vals = []
+    os.environ["OMP_NUM_THREADS"] = str(threads)  # before the oracle's OpenMP runtime starts
+    import numpy as np
+    pyoracle, pyproblems = oracle_mod()
+    og, mask, cents, radii, seed, tol = pyproblems.workload("C3")
+    seq = pyproblems.OUFields((og.nz, og.ny, og.nx), seed, mask)
+    seq.current()
+    rhs = seq.advance()  # step 1 of the OU sequence: the GPU arm's right-hand side
+    times, iters = [], None
     for s in range(args.warmup + args.steps):
-        v, info = cpu_sample(g, rhs, mask, iters, threads)
+        t, x, res = oracle_solve(og, rhs, mask, tol)
         if s >= args.warmup:
-            vals.append(v)
-    value = float(np.mean(vals))
+            times.append(t)
+            iters = res["iters"]
+    sec = float(np.mean(times))
+    value = 1.0 / sec
+    sample = ("each step one complete oracle PCG solve of the C3 workload (256^3, 1000 spheres) from zero to a "
+              "1e-8 true relative residual: %d iterations, %.2f s mean over %d steps" % (iters, sec, len(times)))
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": sec * 1000.0, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": WORKLOAD, "method": "plain FP64 Jacobi PCG (oracle port, OpenMP)"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "per step: oracle PCG at 256^3 for 1 and 6 iterations; per-iteration time "
-                                       "from the difference, scaled to %d iterations (the plain FP64 count "
-                                       "to 1e-8 on this workload)" % iters},
+            "iters": iters,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "cpu": cpu_model(), "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -323,17 +348,33 @@ def run_ours(args):
             rep = step(kw)
             assert rep.status == bbpp.CONVERGED, (name, rep.as_dict())
 
-    # the FP64 solution each method is measured against: this library's plain
-    # FP64 PCG to a 1e-12 true relative residual (the tests pin that solver to
-    # the CPU oracle); its max error is far below the 1e-8 runs' own
-    dref = bbpp.DeviceArray(g.shape, np.float64)
-    rref = s.solve(drhs, dref, dmask, tol=1e-12, precision=bbpp.FP64)
-    assert rref.status == bbpp.CONVERGED
-    xref = dref.download()
+    # The FP64 solution each method is measured against: the CPU oracle's plain
+    # FP64 PCG, from zero to a 1e-8 true relative residual (timed: that solve is
+    # the CPU baseline), then continued from there to 1e-12.  With --no-cpu it is
+    # this library's plain FP64 PCG to 1e-12 instead (the tests pin that solver to
+    # the oracle).
+    cpu = None
+    ref_kind = "library FP64 PCG to a 1e-12 true relative residual"
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        pyoracle, _ = oracle_mod()
+        og = pyoracle.from_tuple(g.as_tuple())
+        t_cpu, x_cpu, r_cpu = oracle_solve(og, rhs, mask, tol)
+        _, xref, r_tight = oracle_solve(og, rhs, mask, 1e-12, x0=x_cpu)
+        cpu = {"value": 1.0 / t_cpu, "unit": UNIT, "cores": threads, "cpu": cpu_model(), "kind": "port",
+               "sample": "one complete oracle PCG solve of this workload from zero to a 1e-8 true relative "
+                         "residual (%d iterations, %.2f s, OpenMP on all host cores)" % (r_cpu["iters"], t_cpu)}
+        ref_kind = "CPU oracle FP64 PCG to a %.1e true relative residual" % r_tight["true_rel"]
+    else:
+        dref = bbpp.DeviceArray(g.shape, np.float64)
+        rref = s.solve(drhs, dref, dmask, tol=1e-12, precision=bbpp.FP64)
+        assert rref.status == bbpp.CONVERGED
+        xref = dref.download()
+        del dref
     xref_max = float(np.abs(xref).max())
-    del dref
 
     res = {}
+    xkeep = {}
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     for name, kw in methods.items():
@@ -349,7 +390,10 @@ def run_ours(args):
         ms = float(np.mean([r.ms for r in reps]))
         ms = vmax(ms)
         # max error of the last solve's x against the FP64 solution (outside the timed loop)
-        err = float(np.abs(dx.download() - xref).max()) / xref_max
+        xlast = dx.download()
+        err = float(np.abs(xlast - xref).max()) / xref_max
+        if name in ("fp64", headline):
+            xkeep[name] = xlast
         res[name] = dict(ms=ms, guess_ms=float(np.mean([r.guess_ms for r in reps])), iters=reps[-1].iters,
                          outer=reps[-1].outer, true_rel=reps[-1].true_rel,
                          max_err_vs_fp64=err, bytes=reps[-1].bytes, launches=int(sum(r.launches for r in reps)),
@@ -411,13 +455,6 @@ def run_ours(args):
     H = res[headline]
     value = aggregate(world, H["ms"])
     plain = res["fp64"]
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        v, info = cpu_sample(g, rhs, mask, plain["iters"], threads)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "oracle PCG at 256^3 for 1 and 6 iterations (t_iter %.3f s); scaled to the %d "
-                         "iterations plain FP64 PCG takes to 1e-8" % (info["t_iter_s"], plain["iters"])}
 
     ref_gpu = reference_gpu(g, mask, rhs, tol, args) if rank == 0 and not args.no_cpu else None
     if ref_gpu is not None and "ms_per_solve" in ref_gpu:
@@ -428,6 +465,13 @@ def run_ours(args):
         ref_gpu["ours_fp64_same_rule"] = {"ms_per_solve": float(np.mean([r.ms for r in reps[1:]])),
                                           "iters": reps[-1].iters}
         ref_gpu["speedup_fp64_same_rule"] = ref_gpu["ms_per_solve"] / ref_gpu["ours_fp64_same_rule"]["ms_per_solve"]
+    if ref_gpu is not None and "_phi" in ref_gpu:
+        phi = ref_gpu.pop("_phi")
+        pmax = float(np.abs(phi).max())
+        ref_gpu["tight"]["true_rel"] = pyoracle_true_rel(g, rhs, phi, mask)
+        # max |x - x_ref| / max |x_ref| of the last timed solve of each method
+        ref_gpu["tight"]["max_err"] = {k: float(np.abs(v - phi).max()) / pmax for k, v in xkeep.items()}
+        ref_gpu["tight"]["oracle_vs_reference_max_err"] = float(np.abs(xref - phi).max()) / pmax
 
     def canon_gbs(r):
         return r["bytes"] / (r["ms"] * 1e-3) / 1e9
@@ -449,8 +493,8 @@ def run_ours(args):
                    "l2": "flushed (512 MB write) before every step; working set 0.9 GB > L2",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "iters": H["iters"], "outer": H["outer"], "true_rel": H["true_rel"],
-        # max |x - x64| / max |x64|, x64 = plain FP64 PCG to a 1e-12 true relative residual
-        "max_err_vs_fp64": H["max_err_vs_fp64"],
+        # max |x - x64| / max |x64|, x64 the FP64 solution named by max_err_reference
+        "max_err_vs_fp64": H["max_err_vs_fp64"], "max_err_reference": ref_kind,
         "plain_fp64": {"value": aggregate(world, plain["ms"]), "ms_per_step": plain["ms"], "iters": plain["iters"],
                        "true_rel": plain["true_rel"], "max_err_vs_fp64": plain["max_err_vs_fp64"],
                        "canonical_gbs": canon_gbs(plain),
@@ -552,8 +596,6 @@ def main():
     ap.add_argument("--only", default=None, choices=["fp64", "ir", "ir_restart", "ir_every50", "ir_warm", "learned_ir",
                                                         "learned_ir_fine"],
                     help="run only warm-up + steps solves of one method (profiler runs)")
-    ap.add_argument("--ref-iters", type=int, default=0,
-                    help="iterations of a full solve for the reference arm (0: the measured C3 count)")
     ap.add_argument("--conv-layers", nargs="*", default=None, metavar="CIN,COUT,N",
                     help="time the forward convolution layers (all, or the ones named) on each kernel instead")
     ap.add_argument("--conv-modes", default="0,1,2", help="convolution kernels to time (0 mma.sync, 1 tm, 2 tx)")
@@ -562,8 +604,6 @@ def main():
     if args.conv_layers is not None:
         conv_layers(args)
     elif args.impl == "reference":
-        if args.ref_iters <= 0:
-            args.ref_iters = C3_FP64_ITERS or 1000
         run_reference(args)
     else:
         run_ours(args)

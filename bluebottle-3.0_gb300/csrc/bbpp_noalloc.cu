@@ -20,15 +20,21 @@
 // the GPU (on different streams, or from different host threads) race on the
 // array, so callers must order them.
 //
-// The first call on a device looks up the device address of the array with
-// cudaGetSymbolAddress while that device is current; make that first call
-// before any stream capture on that device.
+// Host code cannot use the array's name as a device address: on the host it
+// names a stand-in, not device memory.  So every call looks the device address
+// up with cudaGetSymbolAddress while the caller's device is current (a table
+// lookup in the CUDA runtime; it allocates nothing) and passes that address to
+// the kernel.  Looking it up on every call, not once per device, keeps the
+// address valid for the context that is current now, also after a
+// cudaDeviceReset has replaced the one the previous call ran in.  The first
+// call on a device also loads this library's device code there, so make that
+// first call before any stream capture on that device.  Each call waits for
+// its stream (it copies the two norms to the host) before it returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/bbpp.h"
 #include "bbpp_internal.h"
@@ -38,8 +44,6 @@ using namespace bbpp;
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-
 struct NoallocScratch {
   DevState st;
   double partials[3 * BBPP_NOALLOC_MAX_CTAS];
@@ -47,12 +51,7 @@ struct NoallocScratch {
 
 __device__ __align__(256) unsigned char g_scratch[sizeof(NoallocScratch)];
 
-std::mutex g_mu;
-void *g_scratch_dev[kMaxDevices];  // device address of g_scratch, per device
-char g_msg[256];
-
 int fail(int rc, const char *msg) {
-  snprintf(g_msg, sizeof(g_msg), "%s", msg);
   fprintf(stderr, "bbpp_residual_noalloc: %s\n", msg);
   return rc;
 }
@@ -77,23 +76,15 @@ extern "C" int bbpp_residual_noalloc(const bbpp_grid *g, const uint8_t *mask, co
   const int kz = (int)((G.nz + nzc - 1) / nzc);
   const dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)((G.nz + kz - 1) / kz));
 
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-    return fail(BBPP_NO_DEVICE, "no current CUDA device");
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return fail(BBPP_NO_DEVICE, "no current CUDA device");
+  // the device address of the scratch in the context current now
   void *base = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_dev[dev]) {
-      void *p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-      if (e != cudaSuccess || !p) {
-        char m[200];
-        snprintf(m, sizeof(m), "cudaGetSymbolAddress failed on device %d: %s", dev, cudaGetErrorString(e));
-        return fail(BBPP_CUDA_ERROR, m);
-      }
-      g_scratch_dev[dev] = p;
-    }
-    base = g_scratch_dev[dev];
+  const cudaError_t ea = cudaGetSymbolAddress(&base, g_scratch);
+  if (ea != cudaSuccess || !base) {
+    char m[200];
+    snprintf(m, sizeof(m), "cudaGetSymbolAddress failed on device %d: %s", dev, cudaGetErrorString(ea));
+    return fail(BBPP_CUDA_ERROR, m);
   }
   NoallocScratch *sc = reinterpret_cast<NoallocScratch *>(base);
   cudaStream_t s = (cudaStream_t)stream;

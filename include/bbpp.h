@@ -162,9 +162,13 @@ int bbpp_residual(bbpp_ctx *ctx, const uint8_t *mask, const double *rhs, const d
  * partial sums (~200 KB per GPU, kept until exit); grids needing more than
  * BBPP_NOALLOC_MAX_CTAS column tiles of 32x8 cells are rejected
  * (BBPP_BAD_ARG).  Calls share that scratch: calls overlapping on the GPU
- * race.  The first call on a device looks up the scratch address and should
- * come before any stream capture.  mask/rhs/x/r are device pointers; stream
- * is a cudaStream_t or NULL.  rr, bb receive (r,r) and (rhs,rhs). */
+ * race.  Every call looks up the scratch's device address in the context
+ * current at the time (so a cudaDeviceReset between calls is harmless); the
+ * first call on a device also loads the library's device code and should
+ * come before any stream capture.  The call waits for its stream before it
+ * returns (the two norms are copied to the host).  mask/rhs/x/r are device
+ * pointers; stream is a cudaStream_t or NULL.  rr, bb receive (r,r) and
+ * (rhs,rhs). */
 #define BBPP_NOALLOC_MAX_CTAS 8192
 int bbpp_residual_noalloc(const bbpp_grid *g, const uint8_t *mask, const double *rhs,
                           const double *x, double *r, double *rr, double *bb, void *stream);

@@ -58,6 +58,20 @@ double orc_rng_gauss(orc_rng *g)
   return X;
 }
 
+void orc_rng_fill_uniform(unsigned long long seed, long long n, double lo, double hi, double *out)
+{
+  orc_rng g;
+  orc_rng_init(&g, seed);
+  for (long long i = 0; i < n; i++) out[i] = lo + (hi - lo) * orc_rng_dbl(&g);
+}
+
+void orc_rng_fill_gauss(unsigned long long seed, long long n, double *out)
+{
+  orc_rng g;
+  orc_rng_init(&g, seed);
+  for (long long i = 0; i < n; i++) out[i] = orc_rng_gauss(&g);
+}
+
 /* --------------------------------------------------------------- grid ---- */
 int orc_grid_check(const orc_grid *g)
 {

@@ -68,6 +68,11 @@ void orc_rng_init(orc_rng *g, unsigned long long seed);
 unsigned long long orc_rng_u64(orc_rng *g);
 double orc_rng_dbl(orc_rng *g);
 double orc_rng_gauss(orc_rng *g);
+/* n draws of one stream seeded with seed: uniform on [lo, hi) as lo + (hi - lo)
+ * rng_dbl(), or Gaussian by the polar method, in the order the reference's
+ * generator returns them (src/rng.c:78-107).  Synthetic inputs. */
+void orc_rng_fill_uniform(unsigned long long seed, long long n, double lo, double hi, double *out);
+void orc_rng_fill_gauss(unsigned long long seed, long long n, double *out);
 
 int orc_grid_check(const orc_grid *g);
 void orc_invm(const orc_grid *g, double *invM);

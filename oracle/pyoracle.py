@@ -58,6 +58,8 @@ def lib():
         L.orc_rhs_mask_refine.argtypes = [ctypes.POINTER(OrcGrid), P, P]
         L.orc_epilogue.argtypes = [ctypes.POINTER(OrcGrid), P, ctypes.c_double, ctypes.c_double, P, P, P, P, P, P, P,
                                    P, P]
+        L.orc_rng_fill_uniform.argtypes = [ctypes.c_ulonglong, ctypes.c_longlong, ctypes.c_double, ctypes.c_double, P]
+        L.orc_rng_fill_gauss.argtypes = [ctypes.c_ulonglong, ctypes.c_longlong, P]
         L.orc_grid_check.argtypes = [ctypes.POINTER(OrcGrid)]
         L.orc_grid_check.restype = ctypes.c_int
         _L = L
@@ -163,3 +165,17 @@ def epilogue(g, mask, rho_f, dt, phi, us, vs, ws, p0):
                        _p(_c(us, np.float64)), _p(_c(vs, np.float64)), _p(_c(ws, np.float64)),
                        _p(_c(p0, np.float64)), _p(u), _p(v), _p(w), _p(p))
     return u, v, w, p
+
+
+def rng_uniform(seed, n, lo=0.0, hi=1.0):
+    """n draws of the reference's Ranq1 stream for seed, uniform on [lo, hi)."""
+    out = np.empty(int(n), np.float64)
+    lib().orc_rng_fill_uniform(seed, int(n), lo, hi, out.ctypes.data)
+    return out
+
+
+def rng_gauss(seed, n):
+    """n Gaussian draws (polar method) of the reference's Ranq1 stream for seed."""
+    out = np.empty(int(n), np.float64)
+    lib().orc_rng_fill_gauss(seed, int(n), out.ctypes.data)
+    return out

@@ -11,7 +11,7 @@ reference source is written to disk.  cuda_solver.cu is compiled with PP_rhs
 renamed to the harness's PP_rhs_inject so a given right-hand side can be
 injected.
 
-Test infrastructure only; needs the reference tree (default /root/reference).
+Test infrastructure only; needs the reference tree (oracle/refpath.py says where).
 """
 import os
 import re
@@ -20,8 +20,11 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-REF = os.environ.get("BBPP_REFERENCE", "/root/reference")
-SRC = os.path.join(REF, "src")
+sys.path.insert(0, os.path.dirname(HERE))
+import refpath  # noqa: E402
+
+REF = refpath.tree()
+SRC = refpath.src()
 CXX = os.environ.get("CXX", "g++")
 FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-w", "-DDOUBLE", "-DJACOBI",
          "-I", os.path.join(HERE, "shim"), "-I", SRC, "-include", os.path.join(HERE, "shim", "emu_cuda.h")]

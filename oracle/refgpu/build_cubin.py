@@ -11,8 +11,11 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-REF = os.environ.get("BBPP_REFERENCE", "/root/reference")
-SRC = os.path.join(REF, "src")
+sys.path.insert(0, os.path.dirname(HERE))
+import refpath  # noqa: E402
+
+REF = refpath.tree()
+SRC = refpath.src()
 SHIM = os.path.join(HERE, "shim")
 
 

@@ -57,6 +57,36 @@ def test_noalloc_residual_matches_context_residual(bbpp_lib):
     assert abs(rr.value - rr_ref) <= 1e-12 * rr_ref
 
 
+@pytest.mark.parametrize("nx,ny,nz", [(512, 512, 16), (4096, 512, 2)])
+def test_noalloc_residual_z_chunks(bbpp_lib, nx, ny, nz):
+    """Grids whose column tiles times planes exceed the scratch's CTA count:
+    the stencil launch then gives each CTA a chunk of several planes (512^2 x 16:
+    1024 tiles, 2 planes per CTA) or has exactly as many tiles as the scratch
+    holds (4096 x 512: 8192 tiles, both planes in one CTA).  Two calls in a row,
+    against the context residual."""
+    import bbpp
+    from bbpp import problems
+    f = noalloc_fn(bbpp_lib)
+    g = problems.make_grid(nx, "ppn", ny=ny, nz=nz)
+    s = bbpp.Solver(g)
+    rng = np.random.default_rng(nx + nz)
+    for call in range(2):
+        mask = (rng.random(g.shape) < 0.05).astype(np.uint8)
+        b = rng.normal(size=g.shape)
+        x = rng.normal(size=g.shape) * (call + 1)
+        db, dx, dm = bbpp.DeviceArray.from_host(b), bbpp.DeviceArray.from_host(x), bbpp.DeviceArray.from_host(mask)
+        r_ref = bbpp.DeviceArray(g.shape, np.float64)
+        r_new = bbpp.DeviceArray(g.shape, np.float64)
+        rr_ref, bb_ref = s.residual(db, dx, r_ref, dm)
+        rr, bb = ctypes.c_double(-1), ctypes.c_double(-1)
+        rc = f(ctypes.byref(g), dm.ptr, db.ptr, dx.ptr, r_new.ptr, ctypes.byref(rr), ctypes.byref(bb), None)
+        assert rc == bbpp.CONVERGED
+        a, e = r_new.download(), r_ref.download()
+        assert np.abs(a - e).max() <= 1e-13 * np.abs(e).max()
+        assert abs(rr.value - rr_ref) <= 1e-12 * rr_ref
+        assert abs(bb.value - bb_ref) <= 1e-12 * bb_ref
+
+
 def test_noalloc_rejects_oversize_grid(bbpp_lib):
     """A grid needing more CTAs than the scratch holds is refused before any
     device work (the pointers are never touched)."""
