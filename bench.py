@@ -519,6 +519,131 @@ def run_ours(args):
         print(json.dumps(line))
 
 
+C5_METRIC = ("512³ OU sequence (50 solves) time-to-1e-8 residual: learned+mixed vs warm-started plain FP64 PCG, "
+             "one GB300")
+C5_WORKLOAD = ("C5: 512^3 cells, periodic x/y + Neumann z, 4000 spheres r=5 cells (fixed layout), OU-evolved "
+               "k^-11/3 RHS (correlation 0.95 per step), consecutive solves to tol 1e-8 (true rel.)")
+
+
+class DevView:
+    """A CUDA tensor seen by the solver's C ABI (device pointer)."""
+
+    def __init__(self, t):
+        self.t = t
+        self.ptr = t.data_ptr()
+
+
+def run_c5(args):
+    """The combined form at scale: consecutive solves of an OU-evolved sequence
+    on the 512^3 geometry, as the reference's time loop calls its pressure solve
+    once per inner iteration.  Every solve of the headline method starts from
+    the learned guess on the previous pressure and runs FP32 PCG with FP64
+    reliable updates to 1e-8; the baseline is plain FP64 PCG warm-started from
+    its previous solution; FP32/FP64 PCG warm-started from the previous pressure
+    (no network) shows what the network adds.  Each method runs its own
+    sequence from the same first pressure.  One JSON line."""
+    import numpy as np
+    import torch
+    import bbpp
+    from bbpp import problems
+    rank, world, barrier, vmax = dist_init(args.gpus)
+    c = problems.CONFIGS["C5"]
+    nsolves = args.c5_solves
+    g = problems.make_grid(c["n"], c["bc"])
+    t0 = time.time()
+    cents, radii = problems.place_spheres(g, c["nsph"], c["rad"], c["seed"])
+    s = bbpp.Solver(g)
+    dmask = bbpp.DeviceArray(g.shape, np.uint8)
+    s.sphere_mask(cents, radii, dmask)
+    mask = dmask.download()
+    net, net_info = train_c4_net(args)
+    setup_s = time.time() - t0
+    tol = c["tol"]
+    dev = torch.device("cuda")
+    seq = problems.OUSequenceDevice(g.shape, c["seed"], mask, device="cuda")
+    rhs = seq.field()
+    torch.cuda.synchronize()
+    p0 = torch.zeros(g.shape, dtype=torch.float64, device=dev)
+    rep0 = s.solve(DevView(rhs), DevView(p0), dmask, tol=tol, precision=bbpp.FP64)
+    assert rep0.status == bbpp.CONVERGED
+    methods = {
+        "learned_ir": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle),
+        "fp64_warm": dict(precision=bbpp.FP64, guess=bbpp.GUESS_GIVEN),
+        "ir_warm": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_GIVEN),
+    }
+    # per method: the previous solution and the output buffer (the learned
+    # guess reads prev and writes x, so they are two buffers, swapped per step)
+    state = {k: [p0.clone(), torch.empty_like(p0)] for k in methods}
+    rec = {k: [] for k in methods}
+    tight_every = max(1, nsolves // 5)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    for t in range(1, nsolves + 1):
+        rhs = seq.step()
+        torch.cuda.synchronize()
+        xs = {}
+        for name, kw in methods.items():
+            prev, out = state[name]
+            if kw["guess"] == bbpp.GUESS_GIVEN:
+                out.copy_(prev)
+                torch.cuda.synchronize()
+                rep = s.solve(DevView(rhs), DevView(out), dmask, tol=tol, **kw)
+            else:
+                rep = s.solve(DevView(rhs), DevView(out), dmask, tol=tol, prev=prev.data_ptr(), **kw)
+            assert rep.status == bbpp.CONVERGED, (name, t, rep.as_dict())
+            rec[name].append({"ms": rep.ms, "guess_ms": rep.guess_ms, "iters": rep.iters, "true_rel": rep.true_rel,
+                              "launches": rep.launches})
+            state[name] = [out, prev]
+            xs[name] = out
+        # max |x - x_fp64| / max |x_fp64| against the warm-started FP64 solve of the same step
+        base = xs["fp64_warm"]
+        bmax = float(base.abs().max())
+        for name in methods:
+            rec[name][-1]["max_err_vs_fp64"] = float((xs[name] - base).abs().max()) / bmax
+        if t % tight_every == 0 or t == nsolves:
+            # and against FP64 PCG continued to a 1e-11 true relative residual
+            xt = base.clone()
+            torch.cuda.synchronize()
+            rt = s.solve(DevView(rhs), DevView(xt), dmask, tol=1e-11, precision=bbpp.FP64, guess=bbpp.GUESS_GIVEN)
+            tmax = float(xt.abs().max())
+            for name in methods:
+                rec[name][-1]["max_err_vs_tight"] = float((xs[name] - xt).abs().max()) / tmax
+            rec["fp64_warm"][-1]["tight_true_rel"] = rt.true_rel
+            del xt
+    clk = clocks.stop()
+
+    def summary(name):
+        r = rec[name]
+        ms = vmax(float(np.mean([v["ms"] for v in r])))
+        tight = [v["max_err_vs_tight"] for v in r if "max_err_vs_tight" in v]
+        return {"solves_per_s": aggregate(world, ms), "ms_per_solve": ms,
+                "guess_ms": float(np.mean([v["guess_ms"] for v in r])),
+                "iters_mean": float(np.mean([v["iters"] for v in r])), "iters_first": r[0]["iters"],
+                "iters_last": r[-1]["iters"], "true_rel_max": max(v["true_rel"] for v in r),
+                "max_err_vs_fp64_max": max(v["max_err_vs_fp64"] for v in r),
+                "max_err_vs_tight_max": max(tight) if tight else None,
+                "per_solve": [{k: (round(v, 4) if k in ("ms", "guess_ms") else v) for k, v in x.items()} for x in r]}
+
+    res = {k: summary(k) for k in methods}
+    H, B = res["learned_ir"], res["fp64_warm"]
+    line = {"metric": C5_METRIC, "value": H["solves_per_s"], "unit": UNIT, "n_gpus": world, "steps": nsolves,
+            "warmup": 0, "ms_per_step": H["ms_per_solve"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-inner/f64-refined (+bf16 guess)", "data": "synthetic",
+            "config": {"workload": C5_WORKLOAD, "solves": nsolves,
+                       "method": "learned guess from the previous pressure (C4 net, on the grid restricted by 2) + "
+                                 "FP32 Jacobi PCG with FP64 reliable updates",
+                       "baseline": "plain FP64 Jacobi PCG warm-started from its previous solution",
+                       "l2": "not flushed: working set > 4 GB, 30x L2",
+                       "rhs": "OU sequence generated on the GPU (torch generator seeded 5*7919, cuFFT), not timed"},
+            "speedup_vs_fp64_warm": B["ms_per_solve"] / H["ms_per_solve"],
+            "speedup_vs_ir_warm": res["ir_warm"]["ms_per_solve"] / H["ms_per_solve"],
+            "methods": res, "first_solve_fp64_iters": rep0.iters, "learned_training": net_info,
+            "setup_s": round(setup_s, 1), "clocks": clk,
+            "gpu_launches": int(sum(v["launches"] for v in rec["learned_ir"]))}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 # forward layers of the learned guess's network: (cin, cout, n, ldi, ldo, co_off),
 # n^3 volume, input channel stride ldi, output written at channel co_off of ldo
 CONV_LAYERS = [(16, 16, 128, 16, 48, 32), (48, 16, 128, 48, 16, 0), (16, 16, 256, 16, 48, 32),
@@ -596,6 +721,9 @@ def main():
     ap.add_argument("--only", default=None, choices=["fp64", "ir", "ir_restart", "ir_every50", "ir_warm", "learned_ir",
                                                         "learned_ir_fine"],
                     help="run only warm-up + steps solves of one method (profiler runs)")
+    ap.add_argument("--workload", default="C3", choices=["C3", "C5"],
+                    help="C3: the headline 256^3 solve (default); C5: the 512^3 OU sequence")
+    ap.add_argument("--c5-solves", type=int, default=50, help="solves of the C5 sequence")
     ap.add_argument("--conv-layers", nargs="*", default=None, metavar="CIN,COUT,N",
                     help="time the forward convolution layers (all, or the ones named) on each kernel instead")
     ap.add_argument("--conv-modes", default="0,1,2", help="convolution kernels to time (0 mma.sync, 1 tm, 2 tx)")
@@ -605,6 +733,8 @@ def main():
         conv_layers(args)
     elif args.impl == "reference":
         run_reference(args)
+    elif args.workload == "C5":
+        run_c5(args)
     else:
         run_ours(args)
 

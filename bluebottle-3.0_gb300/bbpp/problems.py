@@ -198,3 +198,57 @@ def make_problem(name, n=None, seed=None, with_mask=True):
     else:
         rhs = spectral_rhs(shape, sd, mask)
     return grid, mask, rhs, c["tol"]
+
+
+class OUSequenceDevice:
+    """The same Ornstein-Uhlenbeck right-hand-side sequence generated on the GPU
+    (torch tensors, cuFFT), for grids where the host generator's FFTs and
+    sequential Ranq1 draws would take minutes per field (the 512^3 workload).
+    Same spectrum, correlation and projection as OUSequence; the white noise
+    comes from torch's seeded CUDA generator instead of Ranq1, so the fields
+    are a different draw of the same process.  Fields are float64 CUDA tensors
+    of the grid's shape (z, y, x); mask is a (z, y, x) uint8 array (1 = solid)
+    or None."""
+
+    def __init__(self, shape, seed, mask=None, rho=OU_RHO, device="cuda"):
+        import torch
+        self.torch = torch
+        self.shape, self.rho, self.device = tuple(shape), rho, device
+        self.gen = torch.Generator(device=device)
+        self.gen.manual_seed(int(seed) * 7919)
+        nz, ny, nx = self.shape
+        k = [torch.fft.fftfreq(m, d=1.0 / m, dtype=torch.float64, device=device) for m in (nz, ny, nx)]
+        kmag = torch.sqrt(k[0][:, None, None] ** 2 + k[1][None, :, None] ** 2 + k[2][None, None, :] ** 2)
+        band = (kmag >= 1) & (kmag <= KMAX)
+        self.amp = torch.where(band, kmag.clamp(min=1.0) ** (-11.0 / 6.0), torch.zeros_like(kmag))
+        del kmag, band
+        self.fluid = None
+        if mask is not None:
+            self.fluid = torch.as_tensor(np.ascontiguousarray(mask)).to(device) == 0
+        self.t = 0
+        self.hat = self._noise() * self.amp
+
+    def _noise(self):
+        torch = self.torch
+        re = torch.randn(self.shape, generator=self.gen, dtype=torch.float64, device=self.device)
+        im = torch.randn(self.shape, generator=self.gen, dtype=torch.float64, device=self.device)
+        return torch.complex(re, im)
+
+    def field(self):
+        """The current field: real part, unit RMS, zero on solid cells, zero mean on fluid cells."""
+        torch = self.torch
+        f = torch.fft.ifftn(self.hat).real.contiguous()
+        f /= torch.sqrt(torch.mean(f * f))
+        if self.fluid is None:
+            f -= f.mean()
+        else:
+            f.masked_fill_(~self.fluid, 0.0)
+            f -= self.fluid * (f.sum() / self.fluid.sum())
+        return f
+
+    def step(self):
+        self.t += 1
+        xi = self._noise()
+        xi *= self.amp
+        self.hat.mul_(self.rho).add_(xi, alpha=float(np.sqrt(1 - self.rho ** 2)))
+        return self.field()

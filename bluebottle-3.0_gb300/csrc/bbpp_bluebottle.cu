@@ -431,6 +431,171 @@ __global__ void k_add_const(Shape S, const double *__restrict__ neg_mean, double
   }
 }
 
+// -------------------------------------------------------------- cages --
+// cuda_build_cages (src/cuda_particle.cu:1516-1646) in four launches instead of
+// 2 x nparts serial launches with a host copy each: reset of phase and
+// phase_shell; one block per particle marking the cells of its cage inside it;
+// one block per particle clearing phase_shell on its boundary cells; one pass
+// over the three face arrays writing every flag.  The geometry is the
+// reference kernels' (cage_setup, build_phase, build_phase_shell,
+// src/particle_kernel.cu:134-426) in their evaluation order with no
+// contraction, so the cells marked are the same.  build_phase runs the
+// particles in index order and the last one to contain a cell keeps it, which
+// is the largest index: atomicMax gives that without the order.
+
+struct CageAxis {
+  int s, e, reach;  // first and last cell of the cage (ghosted index), cells the reference's launch reaches
+};
+
+// cage_setup and the clamp of build_phase on one axis: cells [s, e] of a cage
+// of 2 ceil(r/h) + 2 - (n % 2) cells centred on the particle's cell, clamped
+// to the ghosted range [0, n + 1] ([1, n] on a wall), of which the
+// reference's blocks of 8 threads reach ceil(cage / 8) * 8 from s.
+__device__ CageAxis cage_axis(double c, double origin, double h, double rad, int n, bool lo_wall, bool hi_wall) {
+  CageAxis a;
+  const int dim = (int)(2. * ceil(__ddiv_rn(rad, h))) + 2 - n % 2;
+  const double ih = __ddiv_rn(1., h);
+  int s = (int)__dadd_rn(__dsub_rn(round(__dmul_rn(__dsub_rn(c, origin), ih)), 0.5 * dim), 1.0);
+  int e = s + dim;
+  const int lo = lo_wall ? 1 : 0, hi = hi_wall ? n : n + 1;
+  s = s < lo ? lo : (s > hi ? hi : s);
+  e = e < lo ? lo : (e > hi ? hi : e);
+  a.s = s;
+  a.e = e;
+  a.reach = (int)ceil((double)dim * 0.125) * 8;
+  return a;
+}
+
+// floor(|(x, y, z)| / r) < 1 as build_phase evaluates it
+__device__ __forceinline__ bool in_sphere(double x, double y, double z, double irad) {
+  const double d = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+  return floor(__dmul_rn(d, irad)) < 1.0;
+}
+
+// (cell index - 0.5) h - offset: the cell centre relative to the particle
+__device__ __forceinline__ double centre_rel(int i, double h, double off) {
+  return __dsub_rn(__dmul_rn((double)i - 0.5, h), off);
+}
+
+struct CageGeom {
+  int nx, ny, nz;          // interior cells
+  int cx, cy, cz;          // ghosted extents (n + 2)
+  double dx, dy, dz;
+  double xs, ys, zs;       // domain origin
+  int wall[6];             // W, E, S, N, B, T face of a non-periodic direction
+};
+
+// Particle n's centre and radius from the host program's part_struct array
+// (stride BB_PART_STRUCT_BYTES; r, x, y, z at bytes 8, 16, 24, 32).
+__device__ __forceinline__ void part_of(const unsigned char *parts, int n, double &x, double &y, double &z,
+                                        double &r) {
+  const bb_part_head *p = reinterpret_cast<const bb_part_head *>(parts + (size_t)n * BB_PART_STRUCT_BYTES);
+  x = p->x;
+  y = p->y;
+  z = p->z;
+  r = p->r;
+}
+
+__global__ void k_cage_reset(long long ncc, int *__restrict__ phase, int *__restrict__ shell) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncc; c += (long long)gridDim.x * blockDim.x) {
+    phase[c] = -1;
+    shell[c] = 1;
+  }
+}
+
+// pass 0 (build_phase): cells of particle n's cage inside it take n (the largest
+// such n wins); pass 1 (build_phase_shell): cells of n with a face neighbour
+// whose centre lies outside n get phase_shell 0.  blockIdx.x = particle.
+template <int PASS>
+__global__ void __launch_bounds__(256) k_cage(CageGeom G, const unsigned char *__restrict__ parts,
+                                              int *__restrict__ phase, int *__restrict__ shell) {
+  const int n = blockIdx.x;
+  double px, py, pz, pr;
+  part_of(parts, n, px, py, pz, pr);
+  const CageAxis ax = cage_axis(px, G.xs, G.dx, pr, G.nx, G.wall[0], G.wall[1]);
+  const CageAxis ay = cage_axis(py, G.ys, G.dy, pr, G.ny, G.wall[2], G.wall[3]);
+  const CageAxis az = cage_axis(pz, G.zs, G.dz, pr, G.nz, G.wall[4], G.wall[5]);
+  if (ax.s == ax.e || ay.s == ay.e || az.s == az.e) return;
+  const int lx = min(ax.e, ax.s + ax.reach - 1) - ax.s + 1;
+  const int ly = min(ay.e, ay.s + ay.reach - 1) - ay.s + 1;
+  const int lz = min(az.e, az.s + az.reach - 1) - az.s + 1;
+  const double rx = __dsub_rn(px, G.xs), ry = __dsub_rn(py, G.ys), rz = __dsub_rn(pz, G.zs);
+  const double irad = __ddiv_rn(1., pr);
+  const int cells = lx * ly * lz;
+  for (int t = threadIdx.x; t < cells; t += blockDim.x) {
+    const int i = ax.s + t % lx, j = ay.s + (t / lx) % ly, k = az.s + t / (lx * ly);
+    const long long C = i + (long long)G.cx * (j + (long long)G.cy * k);
+    const double xx = centre_rel(i, G.dx, rx), yy = centre_rel(j, G.dy, ry), zz = centre_rel(k, G.dz, rz);
+    if (PASS == 0) {
+      if (in_sphere(xx, yy, zz, irad)) atomicMax(&phase[C], n);
+    } else if (phase[C] == n) {
+      const bool edge = !in_sphere(centre_rel(i - 1, G.dx, rx), yy, zz, irad) ||
+                        !in_sphere(centre_rel(i + 1, G.dx, rx), yy, zz, irad) ||
+                        !in_sphere(xx, centre_rel(j - 1, G.dy, ry), zz, irad) ||
+                        !in_sphere(xx, centre_rel(j + 1, G.dy, ry), zz, irad) ||
+                        !in_sphere(xx, yy, centre_rel(k - 1, G.dz, rz), irad) ||
+                        !in_sphere(xx, yy, centre_rel(k + 1, G.dz, rz), irad);
+      if (edge) shell[C] = 0;
+    }
+  }
+}
+
+// Every face flag of the three face arrays (cage_flag_*, flag_external_*,
+// src/particle_kernel.cu:428-576): on the interior face planes -1 across a
+// phase change or between two shell cells, else 1; the ghost face planes 1;
+// both wall planes of a non-periodic direction 0.  Threads run each array in
+// its own memory order (flag_u [i][k][j], flag_v [j][i][k], flag_w [k][j][i]).
+__global__ void k_cage_flags(CageGeom G, int parts, const int *__restrict__ phase, const int *__restrict__ shell,
+                             int *__restrict__ fu, int *__restrict__ fv, int *__restrict__ fw) {
+  const int cx = G.cx, cy = G.cy, cz = G.cz;
+  const long long nu = (long long)(G.nx + 3) * cz * cy, nv = (long long)(G.ny + 3) * cx * cz,
+                  nw = (long long)(G.nz + 3) * cy * cx;
+  const long long total = nu + nv + nw;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    int a, b, plane, axis;  // (a, b) the in-plane indices in memory order, plane the face index along axis
+    long long c;
+    if (t < nu) {
+      c = t;
+      axis = 0;
+      a = (int)(c % cy);  // j
+      b = (int)((c / cy) % cz);  // k
+      plane = (int)(c / ((long long)cy * cz));  // i
+    } else if (t < nu + nv) {
+      c = t - nu;
+      axis = 1;
+      a = (int)(c % cz);  // k
+      b = (int)((c / cz) % cx);  // i
+      plane = (int)(c / ((long long)cz * cx));  // j
+    } else {
+      c = t - nu - nv;
+      axis = 2;
+      a = (int)(c % cx);  // i
+      b = (int)((c / cx) % cy);  // j
+      plane = (int)(c / ((long long)cx * cy));  // k
+    }
+    const int n = axis == 0 ? G.nx : (axis == 1 ? G.ny : G.nz);
+    int f = 1;
+    if (parts && plane >= 1 && plane <= n + 1) {
+      long long hi, lo;  // the cells on the two sides of the face
+      if (axis == 0) {
+        hi = plane + (long long)cx * (a + (long long)cy * b);
+        lo = hi - 1;
+      } else if (axis == 1) {
+        hi = b + (long long)cx * (plane + (long long)cy * a);
+        lo = hi - cx;
+      } else {
+        hi = a + (long long)cx * (b + (long long)cy * plane);
+        lo = hi - (long long)cx * cy;
+      }
+      const bool flip = ((phase[lo] < 0) != (phase[hi] < 0)) || (shell[hi] < 1 && shell[lo] < 1);
+      f = flip ? -1 : 1;
+    }
+    if (G.wall[2 * axis] && G.wall[2 * axis + 1] && (plane == 1 || plane == n + 1)) f = 0;
+    (axis == 0 ? fu : (axis == 1 ? fv : fw))[c] = f;
+  }
+}
+
 struct Epi {
   double *partials = nullptr;  // one per block of k_update_p, then -mean
   unsigned int *ticket = nullptr;
@@ -509,6 +674,42 @@ extern "C" void cuda_PP_init_jacobi_preconditioner(void) {
     if (rc) fail("bbpp_invm", rc);
   }
   check(cudaDeviceSynchronize(), "preconditioner init");
+}
+
+extern "C" void cuda_build_cages(void) {
+  if (nprocs != 1) {
+    fprintf(stderr, "N%d >> bbpp: one rank per GPU only (nprocs = %d)\n", rank, nprocs);
+    exit(EXIT_FAILURE);
+  }
+  const bb_dom_struct &d = dom[rank];
+  CageGeom G;
+  G.nx = d.Gcc.in;
+  G.ny = d.Gcc.jn;
+  G.nz = d.Gcc.kn;
+  G.cx = G.nx + 2;
+  G.cy = G.ny + 2;
+  G.cz = G.nz + 2;
+  G.dx = d.dx;
+  G.dy = d.dy;
+  G.dz = d.dz;
+  G.xs = d.xs;
+  G.ys = d.ys;
+  G.zs = d.zs;
+  const int b6[6] = {bc.pW, bc.pE, bc.pS, bc.pN, bc.pB, bc.pT};
+  for (int f = 0; f < 6; f++) G.wall[f] = b6[f] != BBPP_PERIODIC;
+  const bool parts = NPARTS > 0;
+  if (parts) {
+    const long long ncc = (long long)G.cx * G.cy * G.cz;
+    k_cage_reset<<<grid_blocks(ncc), 256>>>(ncc, _phase, _phase_shell);
+    if (nparts > 0) {
+      k_cage<0><<<nparts, 256>>>(G, reinterpret_cast<const unsigned char *>(_parts), _phase, _phase_shell);
+      k_cage<1><<<nparts, 256>>>(G, reinterpret_cast<const unsigned char *>(_parts), _phase, _phase_shell);
+    }
+  }
+  const long long nf = (long long)(G.nx + 3) * G.cz * G.cy + (long long)(G.ny + 3) * G.cx * G.cz +
+                       (long long)(G.nz + 3) * G.cy * G.cx;
+  k_cage_flags<<<grid_blocks(nf), 256>>>(G, parts ? 1 : 0, _phase, _phase_shell, _flag_u, _flag_v, _flag_w);
+  check(cudaGetLastError(), "cage kernels");
 }
 
 extern "C" void cuda_PP_cg(void) { solve(true, false); }

@@ -61,6 +61,17 @@ typedef struct bb_bc_pressure {
   int pW, pE, pS, pN, pB, pT;
 } bb_bc_pressure;
 
+/* The leading members of part_struct (src/particle.h:343-348) and its size
+ * with -DDOUBLE and the reference's NNODES 26, MAX_COEFFS 15, S_MAX_COEFFS 25
+ * and MAX_NEIGHBORS 12 (src/particle.h:42-83): the cage builder reads each
+ * particle's radius and centre from the host program's device array _parts,
+ * whose stride is that size. */
+#define BB_PART_STRUCT_BYTES 3128
+typedef struct bb_part_head {
+  int N;
+  bb_real r, x, y, z;
+} bb_part_head;
+
 /* ---- entry points (src/bluebottle.h:3073,3085,3112; defined in the
  * reference at src/cuda_solver.cu:31,38,573) ---- */
 
@@ -94,6 +105,17 @@ void cuda_dom_BC_p(bb_real *array);
 void cuda_project(void);
 void cuda_update_p(void);
 
+/* The phase field and face flags of the particles' cages, same name and
+ * signature as src/cuda_particle.cu:1516 (declared src/cuda_particle.h), one
+ * rank: flags reset to 1; with particles (NPARTS > 0) _phase = the index of the
+ * last particle whose sphere contains the cell centre (else -1), _phase_shell
+ * = 0 on solid cells with a face neighbour outside their particle (else 1), and
+ * the face flags -1 across a phase change or between two shell cells; 0 on
+ * both wall faces of a non-periodic direction.  Reads _parts[0 .. nparts-1]
+ * (the host program's particles, periodic copies included, as the reference's
+ * kernels do).  Four launches on the default stream, whatever nparts. */
+void cuda_build_cages(void);
+
 /* Free the library's private device workspace (no counterpart in the
  * reference, whose solver uses the host program's buffers). */
 void bbpp_bluebottle_release(void);
@@ -115,6 +137,8 @@ extern bb_real *_u_star, *_v_star, *_w_star;
 extern int *_phase;
 extern bb_real *_u, *_v, *_w, *_p, *_p0;  /* the epilogue's fields */
 extern int *_flag_u, *_flag_v, *_flag_w;
+extern int *_phase_shell;
+extern unsigned char *_parts; /* part_struct *, read at stride BB_PART_STRUCT_BYTES */
 /* ---- functions of the host program the solver calls ---- */
 void cuda_part_BC_p(void);                                              /* src/cuda_particle.cu:1679 */
 void recorder_PP(char *name, int niter, bb_real resid, bb_real etime);  /* src/recorder.c:190 */

@@ -496,3 +496,111 @@ void orc_epilogue(const orc_grid *g, const uint8_t *solid, double rho_f, double 
   const double mean = s / (double)n;
   for (long long c = 0; c < n; c++) p[c] += -mean;
 }
+
+/* ------------------------------------------------------------- cages ---- */
+/* The cage of particle n on one axis (cage_setup and the start/end clamp of
+ * build_phase, src/particle_kernel.cu:134-146,158-224): first cell s, last
+ * cell e (inclusive, ghosted index), and the number of cells the launch's
+ * threads reach from s (blocks of 8 threads cover ceil(cage/8) * 8 cells). */
+typedef struct cage_axis { int s, e, reach; } cage_axis;
+
+static cage_axis cage_on_axis(double c, double origin, double h, double rad, int n, int lo_wall, int hi_wall)
+{
+  cage_axis a;
+  const int dim = (int)(2. * ceil(rad / h)) + 2 - n % 2;
+  const double ih = 1. / h;
+  int s = (int)(round((c - origin) * ih) - 0.5 * dim + 1);
+  int e = s + dim;
+  const int lo = lo_wall ? 1 : 0, hi = hi_wall ? n : n + 1;
+  s += (lo - s) * (s < lo) + (hi - s) * (s > hi);
+  e += (lo - e) * (e < lo) + (hi - e) * (e > hi);
+  a.s = s;
+  a.e = e;
+  a.reach = (int)ceil((double)dim * (1. / 8)) * 8;
+  return a;
+}
+
+static int inside_sphere(double xx, double yy, double zz, double irad)
+{
+  const double d = sqrt(xx * xx + yy * yy + zz * zz);
+  return floor(d * irad) < 1;
+}
+
+void orc_build_cages(const orc_grid *g, double xs, double ys, double zs, int with_parts, int nparts,
+                     const double *px, const double *py, const double *pz, const double *pr, int *phase,
+                     int *phase_shell, int *flag_u, int *flag_v, int *flag_w)
+{
+  const int nx = g->nx, ny = g->ny, nz = g->nz;
+  const int cx = nx + 2, cy = ny + 2, cz = nz + 2;          /* ghosted cell extents */
+  const long long ncc = (long long)cx * cy * cz;
+  const long long nfx = (long long)(nx + 3) * cz * cy, nfy = (long long)(ny + 3) * cx * cz,
+                  nfz = (long long)(nz + 3) * cy * cx;
+  for (long long c = 0; c < nfx; c++) flag_u[c] = 1;
+  for (long long c = 0; c < nfy; c++) flag_v[c] = 1;
+  for (long long c = 0; c < nfz; c++) flag_w[c] = 1;
+#define CC(i, j, k) ((i) + (long long)cx * ((j) + (long long)cy * (k)))
+  if (with_parts) {
+    for (long long c = 0; c < ncc; c++) { phase[c] = -1; phase_shell[c] = 1; }
+    for (int pass = 0; pass < 2; pass++)
+      for (int n = 0; n < nparts; n++) {
+        const double rx = px[n] - xs, ry = py[n] - ys, rz = pz[n] - zs, irad = 1. / pr[n];
+        const cage_axis ax = cage_on_axis(px[n], xs, g->dx, pr[n], nx, g->bc[0] != 0, g->bc[1] != 0);
+        const cage_axis ay = cage_on_axis(py[n], ys, g->dy, pr[n], ny, g->bc[2] != 0, g->bc[3] != 0);
+        const cage_axis az = cage_on_axis(pz[n], zs, g->dz, pr[n], nz, g->bc[4] != 0, g->bc[5] != 0);
+        if (ax.s == ax.e || ay.s == ay.e || az.s == az.e || ax.reach <= 0 || ay.reach <= 0 || az.reach <= 0)
+          continue;
+        for (int k = az.s; k <= az.e && k < az.s + az.reach; k++)
+          for (int j = ay.s; j <= ay.e && j < ay.s + ay.reach; j++)
+            for (int i = ax.s; i <= ax.e && i < ax.s + ax.reach; i++) {
+              const long long C = CC(i, j, k);
+              const double xx = (i - 0.5) * g->dx - rx, yy = (j - 0.5) * g->dy - ry, zz = (k - 0.5) * g->dz - rz;
+              if (pass == 0) {
+                if (inside_sphere(xx, yy, zz, irad)) phase[C] = n;
+              } else if (phase[C] == n) {
+                const double xw = (i - 1 - 0.5) * g->dx - rx, xe = (i + 1 - 0.5) * g->dx - rx;
+                const double ysn = (j - 1 - 0.5) * g->dy - ry, yn = (j + 1 - 0.5) * g->dy - ry;
+                const double zb = (k - 1 - 0.5) * g->dz - rz, zt = (k + 1 - 0.5) * g->dz - rz;
+                if (!inside_sphere(xw, yy, zz, irad) || !inside_sphere(xe, yy, zz, irad) ||
+                    !inside_sphere(xx, ysn, zz, irad) || !inside_sphere(xx, yn, zz, irad) ||
+                    !inside_sphere(xx, yy, zb, irad) || !inside_sphere(xx, yy, zt, irad))
+                  phase_shell[C] = 0;
+              }
+            }
+      }
+    /* a face flips to -1 between a fluid and a solid cell, or between two shell cells */
+#define FLIP(a, b) (((phase[a] < 0) != (phase[b] < 0)) || (phase_shell[a] < 1 && phase_shell[b] < 1))
+    for (int k = 0; k < cz; k++)
+      for (int j = 0; j < cy; j++)
+        for (int i = 1; i <= nx + 1; i++)
+          flag_u[j + (long long)cy * (k + (long long)cz * i)] = FLIP(CC(i - 1, j, k), CC(i, j, k)) ? -1 : 1;
+    for (int k = 0; k < cz; k++)
+      for (int j = 1; j <= ny + 1; j++)
+        for (int i = 0; i < cx; i++)
+          flag_v[k + (long long)cz * (i + (long long)cx * j)] = FLIP(CC(i, j - 1, k), CC(i, j, k)) ? -1 : 1;
+    for (int k = 1; k <= nz + 1; k++)
+      for (int j = 0; j < cy; j++)
+        for (int i = 0; i < cx; i++)
+          flag_w[i + (long long)cx * (j + (long long)cy * k)] = FLIP(CC(i, j, k - 1), CC(i, j, k)) ? -1 : 1;
+#undef FLIP
+  }
+#undef CC
+  /* walls of a non-periodic direction: flag 0 on both boundary faces */
+  if (g->bc[0] != 0 && g->bc[1] != 0)
+    for (int k = 0; k < cz; k++)
+      for (int j = 0; j < cy; j++) {
+        flag_u[j + (long long)cy * (k + (long long)cz * 1)] = 0;
+        flag_u[j + (long long)cy * (k + (long long)cz * (nx + 1))] = 0;
+      }
+  if (g->bc[2] != 0 && g->bc[3] != 0)
+    for (int k = 0; k < cz; k++)
+      for (int i = 0; i < cx; i++) {
+        flag_v[k + (long long)cz * (i + (long long)cx * 1)] = 0;
+        flag_v[k + (long long)cz * (i + (long long)cx * (ny + 1))] = 0;
+      }
+  if (g->bc[4] != 0 && g->bc[5] != 0)
+    for (int j = 0; j < cy; j++)
+      for (int i = 0; i < cx; i++) {
+        flag_w[i + (long long)cx * (j + (long long)cy * 1)] = 0;
+        flag_w[i + (long long)cx * (j + (long long)cy * (nz + 1))] = 0;
+      }
+}

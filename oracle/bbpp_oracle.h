@@ -113,6 +113,23 @@ void orc_epilogue(const orc_grid *g, const uint8_t *solid, double rho_f, double 
                   const double *us, const double *vs, const double *ws, const double *p0, double *u, double *v,
                   double *w, double *p);
 
+/* cuda_build_cages (src/cuda_particle.cu:1516-1646) on one rank: flags reset to
+ * 1 (reset_flag_*); with particles, phase = -1 and phase_shell = 1 (reset_phases),
+ * then particle by particle in index order the cells of its cage whose centre
+ * lies inside it take its index (cage_setup, build_phase), then the solid cells
+ * of each particle with a face neighbour centre outside it get phase_shell = 0
+ * (build_phase_shell), then the face flags -1 across a phase change or between
+ * two shell cells, else 1 (cage_flag_*); finally 0 on both wall faces of a
+ * non-periodic direction (flag_external_*).  src/particle_kernel.cu:79-576.
+ * Ghosted layouts of the reference: phase, phase_shell (nx+2)(ny+2)(nz+2) x
+ * fastest; flag_u [i][k][j] over (nx+3)(nz+2)(ny+2); flag_v [j][i][k] over
+ * (ny+3)(nx+2)(nz+2); flag_w [k][j][i] over (nz+3)(ny+2)(nx+2).  Particle
+ * centres in domain coordinates, domain origin (xs, ys, zs); with_parts is the
+ * reference's NPARTS > 0. */
+void orc_build_cages(const orc_grid *g, double xs, double ys, double zs, int with_parts, int nparts,
+                     const double *px, const double *py, const double *pz, const double *pr, int *phase,
+                     int *phase_shell, int *flag_u, int *flag_v, int *flag_w);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,8 @@ def lib():
                                    P, P]
         L.orc_rng_fill_uniform.argtypes = [ctypes.c_ulonglong, ctypes.c_longlong, ctypes.c_double, ctypes.c_double, P]
         L.orc_rng_fill_gauss.argtypes = [ctypes.c_ulonglong, ctypes.c_longlong, P]
+        L.orc_build_cages.argtypes = [ctypes.POINTER(OrcGrid), ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P, P]
         L.orc_grid_check.argtypes = [ctypes.POINTER(OrcGrid)]
         L.orc_grid_check.restype = ctypes.c_int
         _L = L
@@ -179,3 +181,22 @@ def rng_gauss(seed, n):
     out = np.empty(int(n), np.float64)
     lib().orc_rng_fill_gauss(seed, int(n), out.ctypes.data)
     return out
+
+
+def build_cages(g, parts, with_parts=True, origin=(0.0, 0.0, 0.0), phase=None, phase_shell=None):
+    """cuda_build_cages on one rank: parts (n, 4) rows (x, y, z, r); returns the
+    ghosted phase, phase_shell and flag_u, flag_v, flag_w arrays (flat, the
+    reference's layouts).  Without particles phase and phase_shell are left as
+    given (the reference does not touch them then)."""
+    parts = np.ascontiguousarray(np.asarray(parts, np.float64).reshape(-1, 4))
+    cols = [np.ascontiguousarray(parts[:, i]) for i in range(4)]
+    ncc = (g.nx + 2) * (g.ny + 2) * (g.nz + 2)
+    ph = np.full(ncc, -1, np.int32) if phase is None else np.array(phase, np.int32).ravel()
+    sh = np.ones(ncc, np.int32) if phase_shell is None else np.array(phase_shell, np.int32).ravel()
+    fu = np.zeros((g.nx + 3) * (g.nz + 2) * (g.ny + 2), np.int32)
+    fv = np.zeros((g.ny + 3) * (g.nx + 2) * (g.nz + 2), np.int32)
+    fw = np.zeros((g.nz + 3) * (g.ny + 2) * (g.nx + 2), np.int32)
+    ptrs = [c.ctypes.data if len(parts) else None for c in cols]
+    lib().orc_build_cages(ctypes.byref(g), origin[0], origin[1], origin[2], int(bool(with_parts)), len(parts), *ptrs,
+                          ph.ctypes.data, sh.ctypes.data, fu.ctypes.data, fv.ctypes.data, fw.ctypes.data)
+    return ph, sh, fu, fv, fw

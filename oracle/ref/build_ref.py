@@ -1,8 +1,8 @@
 """Host build of the reference pressure solver, used to pin the oracle.
 
-Compiles the unmodified src/cuda_solver.cu, src/solver_kernel.cu and
-src/bluebottle_kernel.cu (the post-solve epilogue's kernels) from the
-reference tree for the CPU, with the shims in oracle/ref/shim (CUDA execution
+Compiles the unmodified src/cuda_solver.cu, src/solver_kernel.cu,
+src/bluebottle_kernel.cu (the post-solve epilogue's kernels) and
+src/particle_kernel.cu (the cage builder's kernels) from the reference tree for the CPU, with the shims in oracle/ref/shim (CUDA execution
 model as fibers, one-rank MPI, thrust::inner_product) and the harness in
 oracle/ref/harness.cpp, into oracle/_ref/libref.so.  Kernel launches
 `k<<<grid, block>>>(args);` are rewritten on the fly, while the source streams
@@ -64,9 +64,15 @@ def rewrite_launches(text):
     return "".join(out)
 
 
+def shared_arrays(text):
+    """`extern __shared__ T name[];` (dynamic shared memory) becomes a static
+    array of 65536 elements: the emulation has no launch-sized shared memory."""
+    return re.sub(r"extern\s+__shared__\s+(\w+)\s+(\w+)\s*\[\s*\]", r"static \1 \2[1 << 16]", text)
+
+
 def compile_ref(src, obj, extra=()):
     text = open(os.path.join(SRC, src)).read()
-    text = rewrite_launches(text)
+    text = rewrite_launches(shared_arrays(text))
     cmd = [CXX] + FLAGS + list(extra) + ["-x", "c++", "-c", "-", "-o", obj]
     r = subprocess.run(cmd, input=text, capture_output=True, text=True)
     if r.returncode != 0:
@@ -86,12 +92,14 @@ def build():
         return None
     os.makedirs(OUT, exist_ok=True)
     objs = [os.path.join(OUT, n) for n in ("cuda_solver.o", "solver_kernel.o", "harness.o", "emu_runtime.o",
-                                           "bluebottle_kernel.o")]
+                                           "bluebottle_kernel.o", "particle_kernel.o", "cages_harness.o")]
     compile_ref("cuda_solver.cu", objs[0], ["-DPP_rhs=PP_rhs_inject"])
     compile_ref("solver_kernel.cu", objs[1])
     compile_ref("bluebottle_kernel.cu", objs[4])
+    compile_ref("particle_kernel.cu", objs[5])  # the cage kernels of cuda_build_cages
     compile_own("harness.cpp", objs[2])
     compile_own("emu_runtime.cpp", objs[3])
+    compile_own("cages_harness.cpp", objs[6])
     lib = os.path.join(OUT, "libref.so")
     r = subprocess.run([CXX, "-shared", "-o", lib] + objs + ["-Wl,--no-undefined", "-lm"], capture_output=True,
                        text=True)

@@ -20,6 +20,8 @@ bb_real *_phi = 0, *_rhs_p = 0, *_invM = 0, *_u_star = 0, *_v_star = 0, *_w_star
 int *_phase = 0;
 bb_real *_u = 0, *_v = 0, *_w = 0, *_p = 0, *_p0 = 0; /* the epilogue's fields */
 int *_flag_u = 0, *_flag_v = 0, *_flag_w = 0;
+int *_phase_shell = 0;         /* the cage builder's outputs */
+unsigned char *_parts = 0;     /* device part_struct array, BB_PART_STRUCT_BYTES per particle */
 
 int stub_niter = -1, stub_calls = 0, stub_timed_calls = 0, stub_init_timed = 0;
 bb_real stub_resid = -1, stub_etime = -1, stub_spmv = -1, stub_up1 = -1;

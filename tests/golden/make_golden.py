@@ -10,8 +10,12 @@ on small seeded inputs, and stores inputs and outputs here as .npz:
   solve_*.npz  rhs, mask, pp_residual, the solution phi and the iteration
                count of cuda_PP_cg / cuda_PP_cg_noparts (stop rule
                (r,z) <= pp_residual^2 (rhs,rhs), residual replacement every 50)
+  cages_*.npz  particle centres and radii, and the phase, phase_shell and face
+               flags cuda_build_cages builds from them (src/cuda_particle.cu:
+               1516-1646 around the kernels of src/particle_kernel.cu:79-576)
 
 Needs the reference tree; run:  python tests/golden/make_golden.py
+(`--only cages` rewrites the cage fixtures alone.)
 """
 import ctypes
 import json
@@ -40,7 +44,73 @@ def load():
     L.ref_solve_u.argtypes = [ctypes.c_double, ctypes.c_double, v, v, v, ctypes.c_double, ctypes.c_int, v, v, v]
     L.ref_epilogue.argtypes = [ctypes.c_double] * 3 + [v] * 10
     L.ref_sizes.argtypes = [v]
+    L.ref_build_cages.argtypes = [ctypes.c_int, ctypes.c_int, v, v, v, v, v, v]
+    L.ref_part_struct_bytes.restype = ctypes.c_longlong
     return L
+
+
+def cage_particles(rng, dims, h, bc, count, rad_cells):
+    """Centres uniform in the box (overlaps allowed: the last index wins a
+    cell), plus, along periodic axes, the shifted copy of every particle within
+    a cage of the boundary -- the ghost particles the host program hands the
+    cage builder of a periodic one-rank domain."""
+    ext = np.array(dims) * np.array(h)
+    rows = []
+    for _ in range(count):
+        c = rng.random(3) * ext
+        r = rad_cells * h[0] * (0.8 + 0.4 * rng.random())
+        rows.append([c[0], c[1], c[2], r])
+    ghosts = []
+    for row in rows:
+        for a in range(3):
+            if bc[2 * a] == P:
+                if row[a] < 2 * row[3]:
+                    g = list(row)
+                    g[a] += ext[a]
+                    ghosts.append(g)
+                elif row[a] > ext[a] - 2 * row[3]:
+                    g = list(row)
+                    g[a] -= ext[a]
+                    ghosts.append(g)
+    return np.array(rows + ghosts, np.float64).reshape(-1, 4)
+
+
+def cages(L, manifest):
+    """Fixtures of cuda_build_cages: seeded particle sets on small one-rank
+    domains; radius 3 cells on an even grid gives cages of 8 cells, the case
+    where the reference's launch reaches one cell short of its cage."""
+    rng = np.random.default_rng(20261204)
+    cases = [
+        ("cages_ppn_16", (16, 14, 12), (P, P, P, P, N, N), 7, 2.4, 1),
+        ("cages_nnn_odd", (15, 13, 11), (N,) * 6, 6, 2.0, 1),
+        ("cages_ppp_r3", (20, 16, 18), (P,) * 6, 5, 3.0, 1),
+        ("cages_pnp_mixed", (17, 12, 14), (P, P, N, N, P, P), 8, 1.6, 1),
+        ("cages_nnp_noparts", (9, 11, 7), (N, N, N, N, P, P), 0, 0, 0),
+    ]
+    for name, dims, bc, count, rad, with_parts in cases:
+        nx, ny, nz = dims
+        h = (1 / nx, 1 / ny, 1 / nz)
+        if name == "cages_ppp_r3":
+            # exact radius of 3 cells (cage of 8 cells)
+            parts = cage_particles(rng, dims, h, bc, count, rad)
+            parts[:, 3] = 3 * h[0]
+        else:
+            parts = cage_particles(rng, dims, h, bc, count, rad)
+        setup(L, dims, h, bc, None)
+        sz = np.zeros(4, np.int64)
+        L.ref_sizes(sz.ctypes.data)
+        phase, shell = np.zeros(sz[0], np.int32), np.zeros(sz[0], np.int32)
+        fu, fv, fw = np.zeros(sz[1], np.int32), np.zeros(sz[2], np.int32), np.zeros(sz[3], np.int32)
+        parts = np.ascontiguousarray(parts)
+        L.ref_build_cages(with_parts, len(parts), parts.ctypes.data if len(parts) else None, phase.ctypes.data,
+                          shell.ctypes.data, fu.ctypes.data, fv.ctypes.data, fw.ctypes.data)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), dims=dims, h=h, bc=bc, with_parts=with_parts,
+                            parts=parts, phase=phase, phase_shell=shell, flag_u=fu, flag_v=fv, flag_w=fw)
+        manifest[name] = {"kind": "cages", "dims": dims, "bc": bc, "nparts": int(len(parts)),
+                          "solid_cells": int((phase > -1).sum()) if with_parts else 0,
+                          "shell_cells": int((shell == 0).sum()) if with_parts else 0,
+                          "part_struct_bytes": int(L.ref_part_struct_bytes())}
+        print(name, len(parts), manifest[name]["solid_cells"], manifest[name]["shell_cells"])
 
 
 def setup(L, dims, h, bc, mask):
@@ -66,6 +136,11 @@ def spheres_mask(dims, h, bc, cents, rads):
 
 def main():
     L = load()
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "cages":
+        manifest = json.load(open(os.path.join(HERE, "manifest.json")))
+        cages(L, manifest)
+        json.dump(manifest, open(os.path.join(HERE, "manifest.json"), "w"), indent=1)
+        return
     rng = np.random.default_rng(20261203)
     manifest = {}
 
@@ -203,6 +278,7 @@ def main():
                             w=layout.fz_from_s3b(wb, dims), p=layout.cells_from_s3b(pb, dims), phi_b=phib)
         manifest[name] = {"kind": "epilogue", "dims": dims, "bc": bc}
         print(name)
+    cages(L, manifest)
     json.dump(manifest, open(os.path.join(HERE, "manifest.json"), "w"), indent=1)
 
 

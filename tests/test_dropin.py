@@ -175,7 +175,7 @@ def test_dropin_exports():
                          check=True).stdout
     syms = {l.split()[-1] for l in out.splitlines() if l.strip()}
     for s in ("cuda_PP_init_jacobi_preconditioner", "cuda_PP_cg", "cuda_PP_cg_noparts", "cuda_PP_cg_timed",
-              "cuda_dom_BC_p", "cuda_project", "cuda_update_p", "bbpp_bluebottle_release"):
+              "cuda_dom_BC_p", "cuda_project", "cuda_update_p", "cuda_build_cages", "bbpp_bluebottle_release"):
         assert s in syms
     und = subprocess.run(["nm", "-D", "-u", bbpp.DROPIN_LIBPATH], capture_output=True, text=True,
                          check=True).stdout
@@ -401,3 +401,63 @@ def test_dropin_epilogue_matches_reference(bbpp_lib, name):
     H.bbpp.lib().bbpp_d2h(b.ctypes.data, pp, b.nbytes)
     p = layout.cells_from_s3b(b, d["dims"])
     assert np.abs(p - d["p"]).max() <= 1e-14 * np.abs(d["p"]).max()
+
+
+# ---------------------------------------------------------- cage builder --
+CAGES = sorted(k for k, v in MANIFEST.items() if v["kind"] == "cages")
+
+
+def test_part_struct_stride_matches_reference():
+    """BB_PART_STRUCT_BYTES (the stride the cage builder reads _parts with)
+    equals sizeof(part_struct) of the reference's own header, as the host build
+    of the reference measured it when the cage fixtures were written."""
+    import re
+    hdr = open(os.path.join(ROOT, "include", "bbpp_bluebottle.h")).read()
+    stride = int(re.search(r"#define BB_PART_STRUCT_BYTES (\d+)", hdr).group(1))
+    assert CAGES and all(MANIFEST[c]["part_struct_bytes"] == stride for c in CAGES)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", CAGES)
+def test_dropin_build_cages_matches_reference(bbpp_lib, name):
+    """cuda_build_cages through the drop-in library, with the host stub's
+    globals, against the reference's cage kernels (golden cages_*.npz):
+    phase, phase_shell and the three face-flag arrays, element for element."""
+    import re
+    d = dict(np.load(os.path.join(GOLD, name + ".npz")))
+    nx, ny, nz = (int(v) for v in d["dims"])
+    H = Host()
+    H.dom = make_dom(nx, ny, nz, tuple(float(v) for v in d["h"]))
+    H.g("dom", ctypes.c_void_p).value = ctypes.addressof(H.dom)
+    bcs = (ctypes.c_int * 6).in_dll(H.stub, "bc")
+    for i, b in enumerate(d["bc"]):
+        bcs[i] = int(b)
+    H.g("rank", ctypes.c_int).value = 0
+    H.g("nprocs", ctypes.c_int).value = 1
+    parts = d["parts"].reshape(-1, 4)
+    with_parts = int(d["with_parts"])
+    H.g("NPARTS", ctypes.c_int).value = with_parts
+    H.g("nparts", ctypes.c_int).value = len(parts)
+    hdr = open(os.path.join(ROOT, "include", "bbpp_bluebottle.h")).read()
+    stride = int(re.search(r"#define BB_PART_STRUCT_BYTES (\d+)", hdr).group(1))
+    raw = np.zeros((max(len(parts), 1), stride), np.uint8)
+    for n, (x, y, z, r) in enumerate(parts):
+        raw[n, 0:4] = np.frombuffer(np.int32(n).tobytes(), np.uint8)
+        raw[n, 8:40] = np.frombuffer(np.array([r, x, y, z], np.float64).tobytes(), np.uint8)
+    H.g("_parts", ctypes.c_void_p).value = H.dev(raw)
+    # outputs start as garbage, except phase and phase_shell without particles,
+    # which the reference leaves as they were
+    keep = with_parts == 0
+    ph0 = d["phase"] if keep else np.full(d["phase"].shape, 7, np.int32)
+    sh0 = d["phase_shell"] if keep else np.full(d["phase_shell"].shape, 7, np.int32)
+    for nm, a in (("_phase", ph0), ("_phase_shell", sh0), ("_flag_u", np.full(d["flag_u"].shape, 7, np.int32)),
+                  ("_flag_v", np.full(d["flag_v"].shape, 7, np.int32)),
+                  ("_flag_w", np.full(d["flag_w"].shape, 7, np.int32))):
+        H.g(nm, ctypes.c_void_p).value = H.dev(np.ascontiguousarray(a, np.int32))
+    H.lib.cuda_build_cages()
+    H.bbpp.sync()
+    for nm, k in (("_phase", "phase"), ("_phase_shell", "phase_shell"), ("_flag_u", "flag_u"), ("_flag_v", "flag_v"),
+                  ("_flag_w", "flag_w")):
+        out = np.empty(d[k].shape, np.int32)
+        H.bbpp.lib().bbpp_d2h(out.ctypes.data, H.g(nm, ctypes.c_void_p).value, out.nbytes)
+        assert np.array_equal(out, d[k]), k

@@ -110,3 +110,27 @@ def test_oracle_epilogue_matches_reference(orc, name):
     for mine, ref in ((u, d["u"]), (v, d["v"]), (w, d["w"]), (p, d["p"])):
         assert mine.shape == ref.shape
         assert np.array_equal(mine, ref)
+
+
+# ----------------------------------------------------- cage builder (CPU)
+@pytest.mark.parametrize("name", names("cages"))
+def test_oracle_build_cages_bit_exact(orc, name):
+    """The oracle's cuda_build_cages restatement against the reference's own
+    cage kernels run through the host build: phase, phase_shell and the three
+    face-flag arrays, element for element."""
+    d = load(name)
+    g = orc.grid(*d["dims"], *d["h"], bc=d["bc"])
+    keep = int(d["with_parts"]) == 0
+    out = orc.build_cages(g, d["parts"], with_parts=not keep, phase=d["phase"] if keep else None,
+                          phase_shell=d["phase_shell"] if keep else None)
+    for a, k in zip(out, ("phase", "phase_shell", "flag_u", "flag_v", "flag_w")):
+        assert np.array_equal(a, d[k]), k
+
+
+def test_cage_fixtures_cover_the_cases():
+    """Overlapping particles, ghost copies across periodic boundaries, walls,
+    odd extents, a particle-free domain."""
+    cases = names("cages")
+    assert len(cases) >= 5
+    assert any(MANIFEST[c]["nparts"] == 0 for c in cases)
+    assert all(MANIFEST[c]["shell_cells"] > 0 for c in cases if MANIFEST[c]["nparts"])
