@@ -36,6 +36,12 @@ NCU_TRAFFIC = {"search_spmv_f32": 226.697984e6 + 150.230784e6, "search_spmv": 43
                "fused_f32": 307.027712e6 + 216.193536e6}
 
 
+# FP64-pipe thread instructions per cell per launch of the plain FP64 kernels on
+# this workload, from one ncu capture of sm__thread_inst_executed_pipe_fp64_pred_on
+# (the summary sits with the other profiles): kernel kind -> instructions per cell
+NCU_FP64_INST = {}
+
+
 def peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -452,6 +458,30 @@ def run_ours(args):
                 "share": kms / tot if tot else None,
                 "peak_source": "measured" if "fallback" not in pk else "fallback"}
 
+    def fp64_roof(name):
+        """The plain FP64 solve against the FP64 pipe it is bound by: FP64 thread
+        instructions of its kernels (per cell, from ncu) over their CUDA-event
+        time, against the FMA rate this GPU issues (bbpp_fp64_fma_rate)."""
+        ks = res[name]["kstats"]
+        if not ks or not fma_rate:
+            return None
+        inst, ms = 0.0, 0.0
+        for kname, nl, kms, _ in ks:
+            if kname in NCU_FP64_INST:
+                inst += NCU_FP64_INST[kname] * N * nl
+                ms += kms
+        if ms == 0.0:
+            return {"peak_fma_per_s": fma_rate, "unit": "FP64 inst/s"}
+        achieved = inst / (ms * 1e-3)
+        return {"bound": "fp64 pipe", "achieved": achieved, "peak": fma_rate, "unit": "FP64 inst/s",
+                "frac": achieved / fma_rate, "inst_per_cell": {k: v for k, v in NCU_FP64_INST.items()},
+                "kernels_ms_share": ms / sum(k[2] for k in ks), "peak_source": "bbpp_fp64_fma_rate (this run)"}
+
+    fma_rate = None
+    try:
+        fma_rate = bbpp.fp64_fma_rate()
+    except Exception:  # noqa: BLE001
+        pass
     H = res[headline]
     value = aggregate(world, H["ms"])
     plain = res["fp64"]
@@ -498,7 +528,8 @@ def run_ours(args):
         "plain_fp64": {"value": aggregate(world, plain["ms"]), "ms_per_step": plain["ms"], "iters": plain["iters"],
                        "true_rel": plain["true_rel"], "max_err_vs_fp64": plain["max_err_vs_fp64"],
                        "canonical_gbs": canon_gbs(plain),
-                       "canonical_frac": canon_gbs(plain) / hb, "roofline": roof("fp64")},
+                       "canonical_frac": canon_gbs(plain) / hb, "roofline": roof("fp64"),
+                       "fp64_roofline": fp64_roof("fp64")},
         "speedup_vs_plain_fp64": plain["ms"] / H["ms"],
         "canonical_gbs": canon_gbs(H),
         "roofline": roof(headline),
@@ -523,14 +554,6 @@ C5_METRIC = ("512³ OU sequence (50 solves) time-to-1e-8 residual: learned+mixed
              "one GB300")
 C5_WORKLOAD = ("C5: 512^3 cells, periodic x/y + Neumann z, 4000 spheres r=5 cells (fixed layout), OU-evolved "
                "k^-11/3 RHS (correlation 0.95 per step), consecutive solves to tol 1e-8 (true rel.)")
-
-
-class DevView:
-    """A CUDA tensor seen by the solver's C ABI (device pointer)."""
-
-    def __init__(self, t):
-        self.t = t
-        self.ptr = t.data_ptr()
 
 
 def run_c5(args):
@@ -564,7 +587,8 @@ def run_c5(args):
     rhs = seq.field()
     torch.cuda.synchronize()
     p0 = torch.zeros(g.shape, dtype=torch.float64, device=dev)
-    rep0 = s.solve(DevView(rhs), DevView(p0), dmask, tol=tol, precision=bbpp.FP64)
+    dv = bbpp.DeviceView.of_tensor  # the solver reads the torch tensors in place
+    rep0 = s.solve(dv(rhs), dv(p0), dmask, tol=tol, precision=bbpp.FP64)
     assert rep0.status == bbpp.CONVERGED
     methods = {
         "learned_ir": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle),
@@ -587,9 +611,9 @@ def run_c5(args):
             if kw["guess"] == bbpp.GUESS_GIVEN:
                 out.copy_(prev)
                 torch.cuda.synchronize()
-                rep = s.solve(DevView(rhs), DevView(out), dmask, tol=tol, **kw)
+                rep = s.solve(dv(rhs), dv(out), dmask, tol=tol, **kw)
             else:
-                rep = s.solve(DevView(rhs), DevView(out), dmask, tol=tol, prev=prev.data_ptr(), **kw)
+                rep = s.solve(dv(rhs), dv(out), dmask, tol=tol, prev=prev.data_ptr(), **kw)
             assert rep.status == bbpp.CONVERGED, (name, t, rep.as_dict())
             rec[name].append({"ms": rep.ms, "guess_ms": rep.guess_ms, "iters": rep.iters, "true_rel": rep.true_rel,
                               "launches": rep.launches})
@@ -604,7 +628,7 @@ def run_c5(args):
             # and against FP64 PCG continued to a 1e-11 true relative residual
             xt = base.clone()
             torch.cuda.synchronize()
-            rt = s.solve(DevView(rhs), DevView(xt), dmask, tol=1e-11, precision=bbpp.FP64, guess=bbpp.GUESS_GIVEN)
+            rt = s.solve(dv(rhs), dv(xt), dmask, tol=1e-11, precision=bbpp.FP64, guess=bbpp.GUESS_GIVEN)
             tmax = float(xt.abs().max())
             for name in methods:
                 rec[name][-1]["max_err_vs_tight"] = float((xs[name] - xt).abs().max()) / tmax

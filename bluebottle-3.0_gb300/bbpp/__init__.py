@@ -123,6 +123,7 @@ def lib():
         "bbpp_memset": (I, [P, I, S]),
         "bbpp_sync": (I, []),
         "bbpp_flush_l2": (I, []),
+        "bbpp_fp64_fma_rate": (I, [ctypes.POINTER(D)]),
         "bbpp_host_alloc": (I, [S, ctypes.POINTER(P)]),
         "bbpp_host_free": (I, [P]),
         "bbpp_kernel_stats": (I, [P, P, I, ctypes.POINTER(I)]),
@@ -146,7 +147,7 @@ def lib():
 def _ptr(a):
     if a is None:
         return None
-    if isinstance(a, DeviceArray):
+    if isinstance(a, (DeviceArray, DeviceView)):
         return a.ptr
     assert isinstance(a, np.ndarray) and a.flags["C_CONTIGUOUS"]
     return a.ctypes.data
@@ -204,6 +205,22 @@ class DeviceArray:
             self.free()
         except Exception:
             pass
+
+
+class DeviceView:
+    """Device memory owned elsewhere (a CUDA tensor of another library, say),
+    passed to the solver by address.  The owner keeps it alive and ordered:
+    work on it must be complete before the solver's call reads it."""
+
+    def __init__(self, ptr, owner=None):
+        self.ptr = int(ptr)
+        self.owner = owner  # kept alive with the view
+
+    @classmethod
+    def of_tensor(cls, t):
+        """A contiguous CUDA tensor (torch) by its data pointer."""
+        assert t.is_cuda and t.is_contiguous()
+        return cls(t.data_ptr(), t)
 
 
 def default_opts(**kw):
@@ -347,6 +364,13 @@ def rng_gauss(seed, n):
 
 def flush_l2():
     _check(lib().bbpp_flush_l2())
+
+
+def fp64_fma_rate():
+    """FP64 FMAs per second of the current GPU (bbpp_fp64_fma_rate)."""
+    v = ctypes.c_double()
+    _check(lib().bbpp_fp64_fma_rate(ctypes.byref(v)))
+    return v.value
 
 
 def sync():

@@ -862,9 +862,15 @@ struct bbpp_net {
        *dP2 = nullptr, *dE2 = nullptr, *dP1 = nullptr, *dE1 = nullptr;
   cudaStream_t stream = nullptr;
   long long launches = 0;  // kernels launched by inference / training
+  // identity of this network and of its workspace, for captured guesses: a
+  // graph holds the workspace's addresses, so it is keyed on both
+  unsigned long long uid = 0, gen = 0;
 };
 
+static unsigned long long g_net_uid = 0;
+
 static void free_work(bbpp_net *n) {
+  n->gen++;
   void *ptrs[] = {n->X0, n->CAT1, n->P1, n->CAT2, n->P2, n->E3, n->D2, n->D1, n->OUT, n->dOUT, n->scales, n->sums,
                   n->lossd, n->dD1, n->G, n->dCAT1, n->dD2, n->dCAT2, n->dE3, n->dP2, n->dE2, n->dP1, n->dE1};
   for (void *p : ptrs)
@@ -1086,6 +1092,7 @@ static unsigned long long rng_next(unsigned long long &v) {  // Ranq1 (src/rng.c
 extern "C" int bbpp_net_create(unsigned long long seed, bbpp_net **out) {
   if (!out) return BBPP_BAD_ARG;
   bbpp_net *n = new bbpp_net();
+  n->uid = __atomic_add_fetch(&g_net_uid, 1ull, __ATOMIC_RELAXED);
   int off = 0;
   for (int l = 0; l < NLAYER; l++) {
     n->L[l] = kLayers[l];
@@ -1383,6 +1390,25 @@ extern "C" int bbpp_conv3_wflip(int cin, int cout, const void *w, void *wt) {
 }
 
 // ------------------------------------------------------ solver hook -------
+// The guess's launches as a CUDA graph: one per (network, buffers, grid,
+// restriction), captured the second time the same guess runs (the first run
+// sizes the network's workspace and builds its tensor maps, which a capture
+// must not do) and replayed after that.
+struct GuessKey {
+  unsigned long long net, gen;  // the network's identity and workspace generation
+  const void *mask, *rhs, *prev, *x;
+  int f, tc, tc_ctas;
+  bool operator==(const GuessKey &o) const {
+    return net == o.net && gen == o.gen && mask == o.mask && rhs == o.rhs && prev == o.prev && x == o.x &&
+           f == o.f && tc == o.tc && tc_ctas == o.tc_ctas;
+  }
+};
+struct GuessGraph {
+  GuessKey key;
+  cudaGraphExec_t exec = nullptr;  // null: seen once, not yet captured
+  long long launches = 0;          // kernels in the graph
+};
+
 struct NetWork {
   double *prev0 = nullptr;  // zero "previous pressure" when none is given
   // the problem restricted by 2: r, p_prev, the network's p0; the solid cells
@@ -1390,7 +1416,14 @@ struct NetWork {
   float *corr = nullptr;  // p0c - pc in FP32 (0 on coarse solid cells)
   uint8_t *mc = nullptr;
   long long ncap = 0;
+  std::vector<GuessGraph> graphs;  // at most 4, oldest dropped first
 };
+
+static void drop_guess_graphs(NetWork *w) {
+  for (auto &g : w->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  w->graphs.clear();
+}
 
 // The learned guess of a solve.  coarsen 2: the network runs on the problem
 // restricted by 2 (k_restrict2) with h^2 scaled by 4, and its correction comes
@@ -1435,35 +1468,93 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
   cudaStream_t saved = n->stream;
   n->stream = ctx->stream;
   cudaEventRecord(e0, ctx->stream);
-  // residual of the warm start into the solver's free Ap buffer (the coarse
-  // path forms it inside its restriction)
-  const double *r = rhs;
-  int rc = 0;
-  if (prev && f == 1) {
-    rc = bbpp_residual_async(ctx, mask, rhs, prev, ctx->Ap);
-    r = ctx->Ap;
-  }
   const double h2 = ctx->grid.dx * ctx->grid.dy;
-  const long long l0 = n->launches;
-  if (f == 2) {
-    NetWork *w = ctx->net;
-    const long long nc = (long long)(nx / 2) * (ny / 2) * (nz / 2);
-    if (rc == 0) {
-      k_resid_restrict2<<<nblocks(nc), 256, 0, ctx->stream>>>(ctx->G, rhs, prev, mask, w->rc, w->pc, w->mc);
-      if (cudaGetLastError() != cudaSuccess) rc = BBPP_CUDA_ERROR;
+  // the guess's launches: residual of the warm start (into the solver's free Ap
+  // buffer; the coarse path forms it inside its restriction), network, and on
+  // the coarse path the correction's interpolation; returns the kernels launched
+  auto body = [&](long long *count) -> int {
+    const long long l0 = n->launches;
+    int rc_ = 0;
+    const double *r = rhs;
+    if (prev && f == 1) {
+      rc_ = bbpp_residual_async(ctx, mask, rhs, prev, ctx->Ap);
+      r = ctx->Ap;
     }
-    if (rc == 0) rc = bbpp_net_infer(n, nx / 2, ny / 2, nz / 2, 4.0 * h2, w->rc, w->pc, mask ? w->mc : nullptr, w->p0c);
-    if (rc == 0) {
-      k_corr2<<<nblocks(nc), 256, 0, ctx->stream>>>(w->corr, w->p0c, w->pc, w->mc, (unsigned)nc);
-      k_prolong2<<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->corr, prev, mask, nx, ny, nz, ctx->G.px, ctx->G.py,
-                                                              ctx->G.pz, x);
-      if (cudaGetLastError() != cudaSuccess) rc = BBPP_CUDA_ERROR;
+    if (f == 2) {
+      NetWork *w = ctx->net;
+      const long long nc = (long long)(nx / 2) * (ny / 2) * (nz / 2);
+      if (rc_ == 0) {
+        k_resid_restrict2<<<nblocks(nc), 256, 0, ctx->stream>>>(ctx->G, rhs, prev, mask, w->rc, w->pc, w->mc);
+        if (cudaGetLastError() != cudaSuccess) rc_ = BBPP_CUDA_ERROR;
+      }
+      if (rc_ == 0)
+        rc_ = bbpp_net_infer(n, nx / 2, ny / 2, nz / 2, 4.0 * h2, w->rc, w->pc, mask ? w->mc : nullptr, w->p0c);
+      if (rc_ == 0) {
+        k_corr2<<<nblocks(nc), 256, 0, ctx->stream>>>(w->corr, w->p0c, w->pc, w->mc, (unsigned)nc);
+        k_prolong2<<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->corr, prev, mask, nx, ny, nz, ctx->G.px, ctx->G.py,
+                                                                ctx->G.pz, x);
+        if (cudaGetLastError() != cudaSuccess) rc_ = BBPP_CUDA_ERROR;
+      }
+      *count = (n->launches - l0) + 3;
+    } else {
+      if (rc_ == 0) rc_ = bbpp_net_infer(n, nx, ny, nz, h2, r, prev, mask, x);
+      *count = (n->launches - l0) + (prev ? 1 : 0);
     }
-    ctx->launches += 3;
-  } else if (rc == 0) {
-    rc = bbpp_net_infer(n, nx, ny, nz, h2, r, prev, mask, x);
+    return rc_;
+  };
+  int rc = 0;
+  long long count = 0;
+  const char *ge = getenv("BBPP_GUESS_GRAPH");
+  if (!ctx->net) ctx->net = new NetWork();
+  NetWork *gw = ctx->net;
+  // the network's workspace for this grid exists before the key is taken
+  if (!(ge && ge[0] == '0')) {
+    const int wnx = f == 2 ? nx / 2 : nx, wny = f == 2 ? ny / 2 : ny, wnz = f == 2 ? nz / 2 : nz;
+    if (!(n->wx == wnx && n->wy == wny && n->wz == wnz && n->wb == 1)) rc = ensure_work(n, wnx, wny, wnz, 1, false);
   }
-  ctx->launches += (n->launches - l0) + (prev && f == 1 ? 1 : 0);
+  const GuessKey key = {n->uid, n->gen, mask, rhs, prev, x, f, conv_tc_mode(), g_tc_max_ctas};
+  GuessGraph *hit = nullptr;
+  for (auto &g : gw->graphs)
+    if (g.key == key) hit = &g;
+  if (rc) {
+    // the workspace could not be made
+  } else if (ge && ge[0] == '0') {
+    rc = body(&count);
+  } else if (hit && hit->exec) {
+    if (cudaGraphLaunch(hit->exec, ctx->stream) != cudaSuccess) rc = BBPP_CUDA_ERROR;
+    count = hit->launches;
+  } else if (hit) {
+    // second run with these buffers: capture, then replay the capture
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      rc = BBPP_CUDA_ERROR;
+    } else {
+      rc = body(&count);
+      const cudaError_t ec = cudaStreamEndCapture(ctx->stream, &graph);
+      if (rc == 0 && ec != cudaSuccess) rc = BBPP_CUDA_ERROR;
+      if (rc == 0 && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = BBPP_CUDA_ERROR;
+      if (graph) cudaGraphDestroy(graph);
+    }
+    if (rc == 0) {
+      hit->exec = exec;
+      hit->launches = count;
+      if (cudaGraphLaunch(exec, ctx->stream) != cudaSuccess) rc = BBPP_CUDA_ERROR;
+    } else {
+      cudaGetLastError();
+      rc = body(&count);  // the capture failed: run the launches directly
+    }
+  } else {
+    rc = body(&count);
+    if (gw->graphs.size() >= 4) {
+      if (gw->graphs.front().exec) cudaGraphExecDestroy(gw->graphs.front().exec);
+      gw->graphs.erase(gw->graphs.begin());
+    }
+    GuessGraph g;
+    g.key = key;
+    gw->graphs.push_back(g);
+  }
+  ctx->launches += count;
   cudaEventRecord(e1, ctx->stream);
   n->stream = saved;
   if (rc == 0) {
@@ -1480,6 +1571,7 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
 
 void bbpp_net_ctx_free(bbpp_ctx *ctx) {
   if (ctx && ctx->net) {
+    drop_guess_graphs(ctx->net);
     if (ctx->net->prev0) cudaFree(ctx->net->prev0);
     cudaFree(ctx->net->rc);
     cudaFree(ctx->net->pc);

@@ -1269,6 +1269,51 @@ extern "C" int bbpp_flush_l2(void) {
   return 0;
 }
 
+// FP64 FMA rate of this GPU: eight independent FMA chains per thread, one
+// wave of 8 CTAs x 256 threads per SM, timed with CUDA events.  The plain
+// FP64 solve is bound by this pipe on parts that issue FP64 at a small
+// fraction of the FP32 rate; its roofline is reported against this number.
+__global__ void __launch_bounds__(256) k_fp64_fma(double *out, int iters, double a, double b) {
+  double v[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = 1e-3 * (threadIdx.x + 1) + k;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = fma(v[k], a, b);
+  }
+  double t = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) t += v[k];
+  if (t == -1.0) out[blockIdx.x] = t;  // never true; keeps the chains live
+}
+
+extern "C" int bbpp_fp64_fma_rate(double *fma_per_s) {
+  bbpp_ctx *ctx = nullptr;
+  if (!fma_per_s) return BBPP_BAD_ARG;
+  const int sms = dev_sms();
+  const int blocks = 8 * sms, threads = 256, iters = 4096;
+  double *out = nullptr;
+  cudaEvent_t e0, e1;
+  CK(cudaMalloc(&out, sizeof(double) * blocks));
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 0.f;
+  for (int rep = 0; rep < 5; rep++) {
+    CK(cudaEventRecord(e0));
+    k_fp64_fma<<<blocks, threads>>>(out, iters, 0.9999999, 1e-7);
+    CK(cudaEventRecord(e1));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep >= 2 && (best == 0.f || ms < best)) best = ms;  // two warm-ups
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *fma_per_s = (double)blocks * threads * iters * 8.0 / (best * 1e-3);
+  return 0;
+}
+
 // ----------------------------------------------------------- kernel stats --
 static const char *kk_name[KK_COUNT] = {"search_spmv", "update", "axpy_x", "resid", "search_spmv_f32",
                                         "update_f32", "axpy_x_f32", "resid_f32", "fused_f32"};

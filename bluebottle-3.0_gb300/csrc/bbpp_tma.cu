@@ -710,6 +710,380 @@ __global__ void __launch_bounds__(TNT) k1_fused(const GeoL G, const __grid_const
   }
 }
 
+// ------------------------------------------------ fused iteration, WS --
+// The fused iteration with its copies issued by a warp of their own.  Warps
+// 0-7 (256 threads) prep and stencil as k1_fused does; warp 8 is the producer:
+// its first lane issues each plane's tensor copies as soon as the stage that
+// plane goes to is released, instead of after the CTA barrier of a plane.
+// Stages are handed back through empty mbarriers, one arrival per compute
+// warp after its last read.  The stencil of plane j takes its lower z
+// neighbour from the centre value the same thread read for plane j - 1 (a
+// register), so a stage is free once the stencil of its own plane is done:
+// with ns stages, plane j + ns is in flight from the end of plane j's stencil,
+// ns - 2 planes ahead of the prep that waits for it.  The compute warps still
+// meet at a barrier of their own once per plane, between the prep of plane
+// j + 1 (rows other threads read) and the stencil of plane j.
+// Arithmetic, order of the partial sums and the stored values are those of
+// k1_fused, so the two kernels give identical results.
+// A wait that runs out marks the CTA (s_bad); later waits then return at once,
+// the producer stops issuing, and at the end the producer waits, with a bound
+// of 10 x the wait limit, for the last copy into every stage before the CTA
+// reports DONE_TIMEOUT and returns, so no copy is in flight when it exits.
+constexpr int WS_WARPS = TNT / 32;       // compute warps
+constexpr int WS_THREADS = TNT + 32;     // plus the producer warp
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// barrier of the compute warps only (named barrier 1, 256 threads)
+__device__ __forceinline__ void compute_sync() { asm volatile("bar.sync 1, %0;" ::"n"(TNT) : "memory"); }
+
+template <int NPT, bool MASK, bool ISO>
+__global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const __grid_constant__ FusedMaps M,
+                                                          float *__restrict__ rout, float *__restrict__ pnew,
+                                                          float *__restrict__ Apout, float *__restrict__ x,
+                                                          const uint8_t *__restrict__ mask, DevState *st,
+                                                          double *partials, int ty, int kz, int ns, int four_d,
+                                                          int l2hint, int pf) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  __shared__ float s_dL[27], s_inv[27];
+  __shared__ double s_red[5 * WS_THREADS / 32];
+  __shared__ unsigned long long s_full[8], s_empty[8];
+  __shared__ int s_bad, s_issued, s_done;
+  pdl_sync();
+  // one read of the state for the whole CTA, so that it returns as a whole
+  if (threadIdx.x == 0) s_done = *(volatile int *)&st->done;
+  __syncthreads();
+  if (s_done) return;
+  const bool first = *(volatile int *)&st->first;
+  const float beta = first ? 0.f : (float)(*(volatile double *)&st->beta);
+  const bool lag = !first && *(volatile int *)&st->dlag;
+  const float alpha = lag ? (float)(*(volatile double *)&st->alpha) : 0.f;
+  const long long wl = *(volatile long long *)&st->wait_ns;
+  const unsigned long long limit = wl > 0 ? (unsigned long long)wl : 1000000000ull;
+  const bool skip_one = *(volatile int *)&st->inject && blockIdx.x == 0 && blockIdx.y == 0;
+  load_tabs<float>(G, s_dL, s_inv);
+  const unsigned long long pol_n = l2_policy(0), pol_stream = l2_policy(l2hint ? 1 : 0);
+  const unsigned long long pol_mask = l2_policy(l2hint ? 2 : 0);
+
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nx = G.nx, ny = G.ny, nz = G.nz;
+  const int nxv = nx >> 2;
+  const int rows = ty + 2;
+  const int arr = rows * nx;
+  float *stage = reinterpret_cast<float *>(smem_raw);  // [ns][3][rows][nx]: r, Ap_old -> p_new, p_old
+  const int y0 = blockIdx.x * ty;
+  const int z0 = blockIdx.y * kz, z1 = min(z0 + kz, nz);
+  const int np = z1 - z0 + 2;
+  const int nj = z1 - z0;
+  const unsigned int plane = (unsigned int)nx * (unsigned int)ny;
+  const unsigned int tx_bytes = (unsigned int)((1 + (lag ? 1 : 0) + (first ? 0 : 1)) * arr * 4);
+  const int ys = G.py ? (y0 - 1 + ny) % ny : y0 - 1;
+  const int yn = G.py ? (y0 + ty) % ny : y0 + ty;
+
+  if (tid == 0) {
+    for (int q = 0; q < ns; q++) {
+      mbar_init(&s_full[q], 1);
+      mbar_init(&s_empty[q], WS_WARPS);
+    }
+    s_bad = 0;
+    s_issued = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  // a bounded wait that gives up at once in a CTA already marked
+  auto wait_phase = [&](unsigned long long *bar, unsigned int parity, unsigned long long lim) -> bool {
+    if (*(volatile int *)&s_bad) return false;
+    if (mbar_wait(bar, parity, lim)) return true;
+    *(volatile int *)&s_bad = 1;
+    return false;
+  };
+
+  bool bad = false;
+  // partial sums: (p,Ap), (r,r), wall part of (r,z) - (r,r), (Ap,z), (Ap,Ap/dL);
+  // zero in the producer warp
+  float s_pap = 0.f, s_rr = 0.f, s_corr = 0.f, s_c1 = 0.f, s_c2 = 0.f;
+  if (tid >= TNT) {
+    // ---- producer warp: lane 0 issues, the warp moves through the planes together
+    int issued = 0;
+    for (int j = 0; j < np; j++) {
+      const int q = j % ns;
+      // lane 0 decides, the warp follows (its lanes stay converged)
+      int ok = 1;
+      if (lane == 0) {
+        if (j >= ns) ok = wait_phase(&s_empty[q], (unsigned int)(j / ns - 1) & 1u, limit);
+        ok = ok && !*(volatile int *)&s_bad;
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        bad = true;
+        break;
+      }
+      if (lane == 0 && !(skip_one && j == 2)) {
+        int zr = z0 - 1 + j;
+        if (G.pz) zr = (zr + nz) % nz;
+        float *rs = stage + (size_t)q * 3 * arr;
+        unsigned long long *bar = &s_full[q];
+        mbar_expect_tx(bar, tx_bytes);
+        load_rows(rs + nx, &M.r_rows, bar, y0, zr, four_d, pol_n);
+        load_rows(rs, &M.r_row, bar, ys, zr, four_d, pol_n);
+        load_rows(rs + (ty + 1) * nx, &M.r_row, bar, yn, zr, four_d, pol_n);
+        if (lag) {
+          float *as = rs + arr;
+          load_rows(as + nx, &M.a_rows, bar, y0, zr, four_d, pol_n);
+          load_rows(as, &M.a_row, bar, ys, zr, four_d, pol_n);
+          load_rows(as + (ty + 1) * nx, &M.a_row, bar, yn, zr, four_d, pol_n);
+        }
+        if (!first) {
+          float *ps = rs + 2 * arr;
+          load_rows(ps + nx, &M.p_rows, bar, y0, zr, four_d, pol_stream);
+          load_rows(ps, &M.p_row, bar, ys, zr, four_d, pol_stream);
+          load_rows(ps + (ty + 1) * nx, &M.p_row, bar, yn, zr, four_d, pol_stream);
+        }
+        const int zp = z0 - 1 + j + pf;
+        if (pf > 0 && zp >= 0 && zp < nz && j + pf < np) {
+          tma_prefetch_rows(&M.r_rows, y0, zp, four_d);
+          if (lag) tma_prefetch_rows(&M.a_rows, y0, zp, four_d);
+          if (!first) tma_prefetch_rows(&M.p_rows, y0, zp, four_d);
+          const size_t c = (size_t)plane * zp + (size_t)nx * y0;
+          if (lag) bulk_prefetch_l2(x + c, (unsigned int)(ty * nx * 4));
+          if (MASK) bulk_prefetch_l2(mask + c, (unsigned int)(ty * nx));
+        }
+      }
+      issued = j + 1;
+      __syncwarp();
+    }
+    if (lane == 0) s_issued = issued;
+  } else {
+    // ---- compute warps
+    auto prep = [&](int j) {
+      const int q = j % ns;
+      if (!wait_phase(&s_full[q], (unsigned int)(j / ns) & 1u, limit)) bad = true;
+      float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)q * 3 * arr);
+      float4 *as = rs + arr / 4;
+      const float4 *ps = rs + 2 * (arr / 4);
+      const int zr = z0 - 1 + j;
+      const int gz = halo_index(zr, nz, G.pz);
+      const int wz = gz >= 0 ? 9 * wall_count(gz, nz, G.pz) : 0;
+      const int nel = rows * nxv;
+      if (G.px && G.py && wz == 0) {
+        for (int e = tid; e < nel; e += TNT) {
+          float4 r = rs[e];
+          if (lag) {
+            const float4 a = as[e];
+            r.x = fmaf(-alpha, a.x, r.x);
+            r.y = fmaf(-alpha, a.y, r.y);
+            r.z = fmaf(-alpha, a.z, r.z);
+            r.w = fmaf(-alpha, a.w, r.w);
+            rs[e] = r;
+          }
+          float4 p = r;
+          if (!first) {
+            const float4 o = ps[e];
+            p.x = fmaf(beta, o.x, r.x);
+            p.y = fmaf(beta, o.y, r.y);
+            p.z = fmaf(beta, o.z, r.z);
+            p.w = fmaf(beta, o.w, r.w);
+          }
+          as[e] = p;
+        }
+      } else {
+        for (int e = tid; e < nel; e += TNT) {
+          const int row = e / nxv, c4 = e - row * nxv;
+          const int gy = halo_index(y0 - 1 + row, ny, G.py);
+          const int wy = gy >= 0 ? 3 * wall_count(gy, ny, G.py) : 0;
+          const int xb = 4 * c4;
+          float4 r = rs[e];
+          if (lag) {
+            const float4 a = as[e];
+            r.x = fmaf(-alpha, a.x, r.x);
+            r.y = fmaf(-alpha, a.y, r.y);
+            r.z = fmaf(-alpha, a.z, r.z);
+            r.w = fmaf(-alpha, a.w, r.w);
+            rs[e] = r;
+          }
+          float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (!first) o = ps[e];
+          float4 p;
+          const float *rr_ = reinterpret_cast<const float *>(&r);
+          const float *oo = reinterpret_cast<const float *>(&o);
+          float *pp = reinterpret_cast<float *>(&p);
+#pragma unroll
+          for (int i = 0; i < 4; i++) {
+            const int cls = wall_count(xb + i, nx, G.px) + wy + wz;
+            const float zv = cls ? rr_[i] * s_inv[cls] : rr_[i];
+            pp[i] = first ? zv : fmaf(beta, oo[i], zv);
+          }
+          as[e] = p;
+        }
+      }
+    };
+
+    int orow[NPT], oc4[NPT];
+#pragma unroll
+    for (int k = 0; k < NPT; k++) {
+      const int e = tid + k * TNT;
+      orow[k] = e / nxv;
+      oc4[k] = e - orow[k] * nxv;
+    }
+    uchar4 mkA[NPT], mkB[NPT];
+    float4 xvA[NPT], xvB[NPT];
+    float4 bv[NPT];  // p_new of the plane below, own cells
+    auto fetch = [&](int zc, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
+#pragma unroll
+      for (int k = 0; k < NPT; k++) {
+        const unsigned int c =
+            plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + orow[k]) + 4u * oc4[k];
+        if (MASK) {
+          const unsigned int m = ld_u32_pol(mask + c, pol_mask);
+          mk[k] = make_uchar4(m & 0xffu, (m >> 8) & 0xffu, (m >> 16) & 0xffu, m >> 24);
+        }
+        if (lag) xv[k] = ld4_pol(reinterpret_cast<const float4 *>(x + c), pol_stream);
+      }
+    };
+
+    auto stencil = [&](int j, const uchar4 (&mk)[NPT], const float4 (&xv)[NPT]) {
+      const int zc = z0 - 1 + j;
+      const float *cr = stage + (size_t)(j % ns) * 3 * arr;       // r_new, plane z
+      const float *cs = cr + arr;                                  // p_new, plane z
+      const float *ts = stage + (size_t)((j + 1) % ns) * 3 * arr + arr;
+      const float *po = cr + 2 * arr;                              // p_old, plane z
+      const int wz = 9 * wall_count(zc, nz, G.pz);
+      const bool interior = G.px && G.py && wz == 0;
+#pragma unroll
+      for (int k = 0; k < NPT; k++) {
+        const int row = orow[k], c4 = oc4[k];
+        const int off = (row + 1) * nx + 4 * c4;
+        const float4 c = *reinterpret_cast<const float4 *>(cs + off);
+        const float4 n = *reinterpret_cast<const float4 *>(cs + off + nx);
+        const float4 s = *reinterpret_cast<const float4 *>(cs + off - nx);
+        const float4 t = *reinterpret_cast<const float4 *>(ts + off);
+        const float4 b = j == 1 ? *reinterpret_cast<const float4 *>(stage + (size_t)((j - 1) % ns) * 3 * arr + arr +
+                                                                     off)
+                                : bv[k];
+        bv[k] = c;
+        float w = __shfl_up_sync(0xffffffffu, c.w, 1);
+        float ea = __shfl_down_sync(0xffffffffu, c.x, 1);
+        if (lane == 0 || c4 == 0) {
+          const int xw = 4 * c4 - 1;
+          w = xw >= 0 ? cs[off - 1] : (G.px ? cs[(row + 1) * nx + nx - 1] : 0.f);
+        }
+        if (lane == 31 || c4 == nxv - 1) {
+          const int xe = 4 * c4 + 4;
+          ea = xe < nx ? cs[off + 4] : (G.px ? cs[(row + 1) * nx] : 0.f);
+        }
+        float a[4];
+        int cls[4] = {0, 0, 0, 0};
+        if (interior) {
+          a[0] = apply_L<float, ISO>(G, s_dL, 0, c.x, c.y, w, n.x, s.x, t.x, b.x);
+          a[1] = apply_L<float, ISO>(G, s_dL, 0, c.y, c.z, c.x, n.y, s.y, t.y, b.y);
+          a[2] = apply_L<float, ISO>(G, s_dL, 0, c.z, c.w, c.y, n.z, s.z, t.z, b.z);
+          a[3] = apply_L<float, ISO>(G, s_dL, 0, c.w, ea, c.z, n.w, s.w, t.w, b.w);
+        } else {
+          const int wy = 3 * wall_count(y0 + row, ny, G.py) + wz;
+          const int xb = 4 * c4;
+#pragma unroll
+          for (int i = 0; i < 4; i++) cls[i] = wall_count(xb + i, nx, G.px) + wy;
+          a[0] = apply_L<float, ISO>(G, s_dL, cls[0], c.x, c.y, w, n.x, s.x, t.x, b.x);
+          a[1] = apply_L<float, ISO>(G, s_dL, cls[1], c.y, c.z, c.x, n.y, s.y, t.y, b.y);
+          a[2] = apply_L<float, ISO>(G, s_dL, cls[2], c.z, c.w, c.y, n.z, s.z, t.z, b.z);
+          a[3] = apply_L<float, ISO>(G, s_dL, cls[3], c.w, ea, c.z, n.w, s.w, t.w, b.w);
+        }
+        if (MASK) {
+          if (mk[k].x) a[0] = 0.f;
+          if (mk[k].y) a[1] = 0.f;
+          if (mk[k].z) a[2] = 0.f;
+          if (mk[k].w) a[3] = 0.f;
+        }
+        const float4 r = *reinterpret_cast<const float4 *>(cr + off);
+        const float rv[4] = {r.x, r.y, r.z, r.w};
+        const float pv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+          s_pap = fmaf(pv[i], a[i], s_pap);
+          s_rr = fmaf(rv[i], rv[i], s_rr);
+          if (interior) {
+            s_c1 = fmaf(a[i], rv[i], s_c1);
+            s_c2 = fmaf(a[i], a[i], s_c2);
+          } else {
+            const float iv = cls[i] ? s_inv[cls[i]] : 1.f;
+            s_corr = fmaf((iv - 1.f) * rv[i], rv[i], s_corr);
+            s_c1 = fmaf(a[i], rv[i] * iv, s_c1);
+            s_c2 = fmaf(a[i] * iv, a[i], s_c2);
+          }
+        }
+        const unsigned int g = plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + row) + 4u * c4;
+        st4_pol(reinterpret_cast<float4 *>(Apout + g), make_float4(a[0], a[1], a[2], a[3]), pol_n);
+        st4_pol(reinterpret_cast<float4 *>(pnew + g), c, pol_stream);
+        st4_pol(reinterpret_cast<float4 *>(rout + g), r, pol_n);
+        if (lag) {
+          const float4 q = *reinterpret_cast<const float4 *>(po + off);
+          float4 xo = xv[k];
+          xo.x = fmaf(alpha, q.x, xo.x);
+          xo.y = fmaf(alpha, q.y, xo.y);
+          xo.z = fmaf(alpha, q.z, xo.z);
+          xo.w = fmaf(alpha, q.w, xo.w);
+          st4_pol(reinterpret_cast<float4 *>(x + g), xo, pol_stream);
+        }
+      }
+    };
+    // hand a stage back to the producer: every lane's reads of it are done
+    auto release = [&](int j) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&s_empty[j % ns]);
+    };
+
+    fetch(z0, mkA, xvA);
+    if (nj >= 2) fetch(z0 + 1, mkB, xvB);
+    prep(0);
+    prep(1);
+    auto step = [&](int j, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
+      prep(j + 1);
+      fence_proxy_async();  // this thread's stage writes before later tensor copies into the stage
+      compute_sync();
+      stencil(j, mk, xv);
+      if (j == 1) release(0);
+      release(j);
+      if (j + 2 <= nj) fetch(z0 + j + 1, mk, xv);
+    };
+    for (int j = 1; j <= nj; j += 2) {
+      step(j, mkA, xvA);
+      if (j + 1 <= nj) step(j + 1, mkB, xvB);
+    }
+  }
+
+  if (__syncthreads_or(bad)) {
+    if (tid == TNT) {
+      // copies issued and maybe still in flight: wait for the last one into every stage
+      const int issued = s_issued;
+      for (int j = max(0, issued - ns); j < issued; j++)
+        if (!(skip_one && j == 2)) mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u, 10ull * limit);
+      atomicExch(&st->done, (int)DONE_TIMEOUT);
+    }
+    return;
+  }
+  double v[5] = {(double)s_pap, (double)s_rr + (double)s_corr, (double)s_rr, (double)s_c1, (double)s_c2}, tot[5];
+  const unsigned int nb = gridDim.x * gridDim.y;
+  const unsigned int bid = blockIdx.x + gridDim.x * blockIdx.y;
+  if (last_cta_reduce<5>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
+    st->fq += 1;
+    if (lag) finish_deferred(st, tot[1], tot[2]);  // r_{q-1} ends iteration q - 1
+    st->dlag = 0;
+    if (st->done == RUNNING || st->done == DONE_PENDING) {
+      const double rz = st->rz, pap = tot[0];
+      const double a = rz / pap;
+      st->pAp = pap;
+      st->alpha = a;
+      st->beta = (rz - 2.0 * a * tot[3] + a * a * tot[4]) / rz;
+      st->first = 0;
+      st->dlag = 1;
+      decide_replacement(st);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ host --
 namespace {
 
@@ -770,6 +1144,7 @@ template <int NPT, bool MASK, bool ISO>
 void set_smem_attr() {
   cudaFuncSetAttribute(k1_tma<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes);
   cudaFuncSetAttribute(k1_fused<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes);
+  cudaFuncSetAttribute(k1_fused_ws<NPT, MASK, ISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxStageBytes);
 }
 
 int env_int(const char *name, int dflt) {
@@ -790,6 +1165,10 @@ struct bbpp_tma_state {
   bool fok = false;
   int fkz = 0, fsmem = 0, pf = 0;
   dim3 fgrid;
+  // its warp-specialised form (k1_fused_ws): own ring depth, smem and wave
+  bool wok = false;
+  int wns = 0, wkz = 0, wsmem = 0;
+  dim3 wgrid;
   std::vector<MapPair> maps;
 };
 
@@ -882,6 +1261,29 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
     chunking(fper, &t->fkz, &t->fgrid);
     t->fok = true;
   }
+  // the warp-specialised form: a stage is free once its own plane's stencil
+  // is done, so 3 stages already keep one plane in flight (BBPP_WS_NS, 3..8)
+  if (t->fok && env_int("BBPP_FUSED_WS", 0)) {
+    int wns = std::max(3, std::min(8, env_int("BBPP_WS_NS", 4)));
+    while (wns > 3 && wns * 3 * (ty + 2) * nx * 4 > kMaxStageBytes) wns--;
+    const int wsmem = wns * 3 * (ty + 2) * nx * 4;
+    int wper = 0;
+    if (wsmem <= kMaxStageBytes) {
+#define BBPP_WS_OCC(N) \
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&wper, k1_fused_ws<N, true, true>, WS_THREADS, wsmem);
+      if (npt == 1) { BBPP_WS_OCC(1) }
+      else if (npt == 2) { BBPP_WS_OCC(2) }
+      else { BBPP_WS_OCC(4) }
+#undef BBPP_WS_OCC
+      cudaGetLastError();
+    }
+    if (wper >= 1) {
+      t->wns = wns;
+      t->wsmem = wsmem;
+      chunking(wper, &t->wkz, &t->wgrid);
+      t->wok = true;
+    }
+  }
 }
 
 void bbpp_tma_free(bbpp_ctx *ctx) {
@@ -902,6 +1304,7 @@ size_t bbpp_tma_partials(const bbpp_ctx *ctx) {
   size_t n = (size_t)ctx->tma->grid.x * ctx->tma->grid.y;
   // the fused kernel sums five products per CTA into room for three per CTA
   if (ctx->tma->fok) n = std::max(n, ((size_t)ctx->tma->fgrid.x * ctx->tma->fgrid.y * 5 + 2) / 3);
+  if (ctx->tma->wok) n = std::max(n, ((size_t)ctx->tma->wgrid.x * ctx->tma->wgrid.y * 5 + 2) / 3);
   return n;
 }
 
@@ -948,9 +1351,13 @@ bool bbpp_tma_fused(bbpp_ctx *ctx, const uint8_t *mask, const float *rin, const 
   M.a_row = ma.row;
   M.p_rows = mp.rows;
   M.p_row = mp.row;
-#define BBPP_FUSED_LAUNCH(N, MK, IS)                                                                             \
-  bbpp_launch(ctx, k1_fused<N, MK, IS>, t->fgrid, dim3(TNT), (size_t)t->fsmem, ctx->GL, M, rout, pnew, apout, x, \
-              mask, st, ctx->partials, t->ty, t->fkz, t->ns, t->four_d, (int)ctx->l2hint, t->pf)
+#define BBPP_FUSED_LAUNCH(N, MK, IS)                                                                              \
+  if (t->wok)                                                                                                     \
+    bbpp_launch(ctx, k1_fused_ws<N, MK, IS>, t->wgrid, dim3(WS_THREADS), (size_t)t->wsmem, ctx->GL, M, rout, pnew, \
+                apout, x, mask, st, ctx->partials, t->ty, t->wkz, t->wns, t->four_d, (int)ctx->l2hint, t->pf);     \
+  else                                                                                                            \
+    bbpp_launch(ctx, k1_fused<N, MK, IS>, t->fgrid, dim3(TNT), (size_t)t->fsmem, ctx->GL, M, rout, pnew, apout, x,  \
+                mask, st, ctx->partials, t->ty, t->fkz, t->ns, t->four_d, (int)ctx->l2hint, t->pf)
 #define BBPP_FUSED_NPT(N)                              \
   if (mask) {                                          \
     if (ctx->GL.iso) BBPP_FUSED_LAUNCH(N, true, true);   \

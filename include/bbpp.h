@@ -190,6 +190,11 @@ int bbpp_memset(void *dst, int value, size_t bytes);
 int bbpp_sync(void);
 /* Fill a buffer larger than L2 to evict cached lines between timed runs. */
 int bbpp_flush_l2(void);
+/* FP64 fused multiply-adds per second this GPU issues (eight independent FMA
+ * chains per thread, a full wave, best of three timed launches): the peak the
+ * plain FP64 solve's roofline is reported against.  No counterpart in the
+ * reference. */
+int bbpp_fp64_fma_rate(double *fma_per_s);
 /* Page-locked host memory (for end-to-end timing from pinned buffers). */
 int bbpp_host_alloc(size_t bytes, void **ptr);
 int bbpp_host_free(void *ptr);

@@ -81,3 +81,99 @@ def test_model_matches_kernel_source():
     assert re.search(r"for \(int j = max\(0, np - ns\); j < np; j\+\+\) mbar_wait", body)
     # the host keeps the ring at 4..8 stages
     assert "ns = std::max(4, std::min(8, ns));" in src
+
+
+# ------------------------------------------------ warp-specialised form ----
+def replay_ws(ns, nj, eager):
+    """k1_fused_ws: a producer issues plane j into stage j % ns once plane
+    j - ns is released (empty barrier, one phase per release); the compute
+    warps prep planes 0 and 1, then per step j prep plane j + 1, stencil plane
+    j (reads planes j and j + 1; plane j - 1 only at j = 1, later from a
+    register) and release plane j (and plane 0 after step 1).  The producer
+    runs as far as it can before every consumer wait (eager) or only when the
+    consumer would block (lazy).  Checks: no deadlock, every plane issued once
+    into a released stage, every wait and release on the phase the kernel's
+    parity names, and no read of a plane after its release."""
+    np_ = nj + 2
+    stage = [None] * ns          # plane a stage holds
+    full_done = [0] * ns         # completed phases of each stage's full barrier
+    empty_done = [0] * ns        # completed phases of each stage's empty barrier
+    released = set()
+    nxt = [0]                    # next plane the producer issues
+
+    def produce_one():
+        j = nxt[0]
+        if j >= np_:
+            return False
+        s = j % ns
+        if j >= ns:
+            # the kernel waits for parity (j / ns - 1) & 1: the (j/ns - 1)-th completion
+            if empty_done[s] < j // ns:
+                return False
+            assert empty_done[s] == j // ns and ((empty_done[s] - 1) & 1) == ((j // ns - 1) & 1)
+            assert (j - ns) in released, "plane %d issued over unreleased plane %d" % (j, j - ns)
+        stage[s] = j
+        full_done[s] += 1        # the copy lands (completes one phase)
+        nxt[0] += 1
+        return True
+
+    def run_producer():
+        while produce_one():
+            pass
+
+    def wait_full(p):
+        if eager:
+            run_producer()
+        while stage[p % ns] != p:
+            assert produce_one(), "deadlock: plane %d never issued" % p
+        assert full_done[p % ns] - 1 == p // ns  # parity (p / ns) & 1 names this phase
+
+    def read(p):
+        assert p not in released, "plane %d read after release" % p
+        assert stage[p % ns] == p
+
+    def release(p):
+        released.add(p)
+        empty_done[p % ns] += 1
+
+    wait_full(0)
+    read(0)
+    wait_full(1)
+    read(1)
+    for j in range(1, nj + 1):
+        wait_full(j + 1)
+        read(j + 1)                # prep
+        for p in (j, j + 1):       # stencil
+            read(p)
+        if j == 1:
+            read(0)
+            release(0)
+        release(j)
+    run_producer()
+    assert nxt[0] == np_
+
+
+@pytest.mark.parametrize("ns", [3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("eager", [True, False])
+def test_ws_ring_schedule(ns, eager):
+    for nj in range(1, 70):
+        replay_ws(ns, nj, eager)
+
+
+def test_ws_two_stages_deadlock():
+    """Two stages: plane 2 needs plane 0's stage, released only after the
+    stencil of plane 1, which waits for plane 2 first -- the host keeps ns >= 3."""
+    with pytest.raises(AssertionError, match="deadlock"):
+        replay_ws(2, 5, False)
+
+
+def test_ws_model_matches_kernel_source():
+    src = open(os.path.join(os.path.dirname(__file__), "..", "bluebottle-3.0_gb300", "csrc", "bbpp_tma.cu")).read()
+    body = src[src.index("k1_fused_ws(const GeoL G"):]
+    body = body[:body.index("// ------------------------------------------------------------------ host --")]
+    assert "if (j >= ns) ok = wait_phase(&s_empty[q], (unsigned int)(j / ns - 1) & 1u, limit);" in body
+    assert "if (!wait_phase(&s_full[q], (unsigned int)(j / ns) & 1u, limit)) bad = true;" in body
+    assert "if (j == 1) release(0);\n      release(j);" in body
+    assert "mbar_init(&s_empty[q], WS_WARPS);" in body
+    assert "const float4 b = j == 1 ?" in body
+    assert "int wns = std::max(3, std::min(8, env_int(\"BBPP_WS_NS\", 4)));" in src

@@ -17,12 +17,6 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-class DevView:
-    def __init__(self, t):
-        self.t = t
-        self.ptr = t.data_ptr()
-
-
 def test_c5_sequence_converges(bbpp_lib):
     import torch
     import bbpp
@@ -46,7 +40,8 @@ def test_c5_sequence_converges(bbpp_lib):
     rhs = seq.field()
     torch.cuda.synchronize()
     p0 = torch.zeros(g.shape, dtype=torch.float64, device="cuda")
-    rep = s.solve(DevView(rhs), DevView(p0), dmask, tol=c["tol"], precision=bbpp.FP64)
+    dv = bbpp.DeviceView.of_tensor  # the solver reads the torch tensors in place
+    rep = s.solve(dv(rhs), dv(p0), dmask, tol=c["tol"], precision=bbpp.FP64)
     assert rep.status == bbpp.CONVERGED and rep.true_rel <= c["tol"]
     methods = {"learned_ir": dict(precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle),
                "fp64_warm": dict(precision=bbpp.FP64, guess=bbpp.GUESS_GIVEN),
@@ -61,9 +56,9 @@ def test_c5_sequence_converges(bbpp_lib):
             if kw["guess"] == bbpp.GUESS_GIVEN:
                 x.copy_(prev)
                 torch.cuda.synchronize()
-                rep = s.solve(DevView(rhs), DevView(x), dmask, tol=c["tol"], **kw)
+                rep = s.solve(dv(rhs), dv(x), dmask, tol=c["tol"], **kw)
             else:
-                rep = s.solve(DevView(rhs), DevView(x), dmask, tol=c["tol"], prev=prev.data_ptr(), **kw)
+                rep = s.solve(dv(rhs), dv(x), dmask, tol=c["tol"], prev=prev.data_ptr(), **kw)
             assert rep.status == bbpp.CONVERGED, (name, t, rep.as_dict())
             assert rep.true_rel <= c["tol"] * 1.0001, (name, t, rep.true_rel)
             out[name] = x

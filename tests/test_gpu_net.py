@@ -176,6 +176,43 @@ def test_net_gradient_matches_cpu_reference(bbpp_lib):
         off += n
 
 
+@pytest.mark.parametrize("layer", range(len(NO.LAYERS)))
+def test_net_gradient_finite_differences(bbpp_lib, layer):
+    """The GPU gradient of each layer against central differences of the GPU's
+    own loss: for a random direction v over the layer's weights and bias,
+    (L(w + eps v) - L(w - eps v)) / (2 eps) against g . v.  Weights and
+    activations are BF16, so the loss is piecewise constant at the scale of a
+    BF16 step: v is as large as the layer's weights (RMS) and eps 1e-2, so
+    every weight moves by about one BF16 step or more and the rounding of the
+    many voxels' activations averages out; the tolerance is 5% of |g . v| (a
+    systematically biased layer gradient of a few percent in the direction
+    tested fails it)."""
+    net = learned.Net(seed=3)
+    p = net.get_params()
+    rhs, prev, tgt, mask = _small_problem(2)
+    dims = (16, 16, 8)
+    d = [bbpp.DeviceArray.from_host(a) for a in (rhs, prev, tgt, mask)]
+    h2 = 1.0 / 256.0
+    _, g = net.loss_grad(dims, h2, *d)
+    off = sum(27 * ci * co + co for ci, co in NO.LAYERS[:layer])
+    ci, co = NO.LAYERS[layer]
+    n = 27 * ci * co + co
+    rng = np.random.default_rng(100 + layer)
+    v = np.zeros_like(p)
+    rms = float(np.sqrt(np.mean(p[off:off + n] ** 2)))
+    v[off:off + n] = rng.normal(size=n).astype(np.float32) * rms
+    eps = 1e-2
+    net.set_params(p + eps * v)
+    lp, _ = net.loss_grad(dims, h2, *d, grads=False)
+    net.set_params(p - eps * v)
+    lm, _ = net.loss_grad(dims, h2, *d, grads=False)
+    net.set_params(p)
+    fd = (lp - lm) / (2 * eps)
+    an = float(np.dot(g.astype(np.float64), v.astype(np.float64)))
+    print("layer %d: finite difference %.6e, gradient %.6e" % (layer, fd, an))
+    assert abs(fd - an) <= 0.05 * abs(an), (fd, an)
+
+
 def test_net_training_lowers_loss(bbpp_lib):
     data, g, _ = learned.make_ou_dataset(16, 24, nsph=4, rad=2.0, seed=5, tol=1e-10)
     net = learned.Net(seed=4)
@@ -284,3 +321,42 @@ def test_learned_guess_gain(bbpp_lib):
     z, w, l = (np.mean(res[k]) for k in ("zero", "warm", "learned"))
     print("iterations zero %.1f warm %.1f learned %.1f" % (z, w, l))
     assert l < z  # the trained guess saves PCG iterations over the zero guess
+
+
+@pytest.mark.parametrize("coarsen", [1, 2])
+def test_guess_graph_replays_match_direct_launches(bbpp_lib, monkeypatch, coarsen):
+    """The learned guess runs directly the first time a set of buffers is seen,
+    is captured as a CUDA graph the second time and replayed after that.  Three
+    guesses with new inputs in the same buffers through that path equal, bit for
+    bit, the same guesses launched directly (BBPP_GUESS_GRAPH=0)."""
+    nx, ny, nz = 32, 16, 24
+    g = problems.make_grid(nx, "ppn", ny=ny, nz=nz)
+    rng = np.random.default_rng(17)
+    mask = np.zeros((nz, ny, nx), np.uint8)
+    mask[6:11, 3:8, 10:17] = 1
+    s = bbpp.Solver(g)
+    net = learned.Net(seed=4)
+    dmask = bbpp.DeviceArray.from_host(mask)
+    drhs, dprev = bbpp.DeviceArray((nz, ny, nx), np.float64), bbpp.DeviceArray((nz, ny, nx), np.float64)
+    dx = bbpp.DeviceArray((nz, ny, nx), np.float64)
+    inputs = []
+    for _ in range(3):
+        rhs = rng.normal(size=(nz, ny, nx))
+        rhs[mask == 1] = 0
+        inputs.append((rhs, rng.normal(size=(nz, ny, nx))))
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("BBPP_GUESS_GRAPH", mode)
+        res = []
+        for rhs, prev in inputs:
+            drhs.upload(rhs)
+            dprev.upload(prev)
+            rep = s.solve(drhs, dx, dmask, tol=1e300, precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED,
+                          net=net.handle, prev=dprev.ptr, net_coarsen=coarsen)
+            assert rep.iters == 0 and rep.launches > 0
+            res.append(dx.download())
+        out[mode] = res
+    for a, b in zip(out["1"], out["0"]):
+        assert np.array_equal(a, b)
+    assert not np.array_equal(out["1"][0], out["1"][1])
+    net.close()

@@ -256,3 +256,25 @@ def test_solve_odd_shapes(lib, orc, dims, bc, precision, ir_mode):
         x, xo = x - x.mean(), xo - xo.mean()
     err = np.abs(x - xo).max() / max(np.abs(xo).max(), 1e-300)
     assert err < 1e4 * tol, err
+
+
+@pytest.mark.parametrize("name,n,bc", [("C3", 128, None), ("C1", 64, None), ("C2", 64, "nnn")])
+@pytest.mark.parametrize("ws_ns", ["3", "4", "6"])
+def test_ws_fused_kernel_bit_identical(lib, name, n, bc, ws_ns, monkeypatch):
+    """The warp-specialised fused kernel (producer warp, empty barriers, lower
+    z neighbour from a register) against the fused kernel it replaces, chosen
+    per context when it is created: the same iterations and a bit-identical
+    solution, for ring depths of 3, 4 and 6 stages."""
+    g, mask, rhs, _ = problems.make_problem(name, n=n)
+    if bc is not None:
+        g = problems.make_grid(n, bc)
+    monkeypatch.setenv("BBPP_FUSED_WS", "0")
+    s_old = bbpp.Solver(g)
+    monkeypatch.setenv("BBPP_FUSED_WS", "1")
+    monkeypatch.setenv("BBPP_WS_NS", ws_ns)
+    s_ws = bbpp.Solver(g)
+    x0, r0 = s_old.solve_host(rhs, mask, tol=1e-8, precision=bbpp.FP32_IR)
+    x1, r1 = s_ws.solve_host(rhs, mask, tol=1e-8, precision=bbpp.FP32_IR)
+    assert r0.status == r1.status == bbpp.CONVERGED
+    assert r0.iters == r1.iters and r0.outer == r1.outer
+    assert np.array_equal(x0, x1)
