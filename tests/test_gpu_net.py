@@ -166,51 +166,57 @@ def test_net_gradient_matches_cpu_reference(bbpp_lib):
     cos = float(g @ gr / (np.linalg.norm(g) * np.linalg.norm(gr)))
     assert cos > 0.99, cos
     assert np.linalg.norm(g - gr) <= 0.1 * np.linalg.norm(gr)
-    # every layer's gradient, not only the largest
+    # every layer's gradient, not only the largest: direction and magnitude
     off = 0
     for cin, cout in NO.LAYERS:
         n = 27 * cin * cout + cout
         a, b = g[off:off + n], gr[off:off + n]
         if np.linalg.norm(b) > 0:
             assert float(a @ b / (np.linalg.norm(a) * np.linalg.norm(b))) > 0.98
+            ratio = float(np.linalg.norm(a) / np.linalg.norm(b))
+            print("layer %d->%d: norm ratio %.4f" % (cin, cout, ratio))
+            assert abs(ratio - 1.0) <= 0.05, ratio  # a scaled layer gradient keeps its cosine, not its norm
         off += n
 
 
 @pytest.mark.parametrize("layer", range(len(NO.LAYERS)))
 def test_net_gradient_finite_differences(bbpp_lib, layer):
-    """The GPU gradient of each layer against central differences of the GPU's
-    own loss: for a random direction v over the layer's weights and bias,
-    (L(w + eps v) - L(w - eps v)) / (2 eps) against g . v.  Weights and
-    activations are BF16, so the loss is piecewise constant at the scale of a
-    BF16 step: v is as large as the layer's weights (RMS) and eps 1e-2, so
-    every weight moves by about one BF16 step or more and the rounding of the
-    many voxels' activations averages out; the tolerance is 5% of |g . v| (a
-    systematically biased layer gradient of a few percent in the direction
-    tested fails it)."""
+    """The GPU gradient of each layer against finite differences of the GPU's
+    own loss.  Weights and activations are BF16, so the loss is piecewise
+    constant on the scale of a BF16 step and a two-point difference of single
+    weights measures rounding, not slope.  The check therefore moves a whole
+    layer along its own weights, w -> (1 + t) w (and its bias), at 41 points
+    t in [-0.05, 0.05], and takes the slope at t = 0 of a cubic fitted to the
+    losses, against g . w.  On the network oracle (FP32 with the same BF16
+    rounding) this estimate lands within 10% of its autograd slope for every
+    layer at this volume, so the bound is 15%: a layer gradient off in sign, by
+    a factor, or missing a term fails it."""
     net = learned.Net(seed=3)
     p = net.get_params()
-    rhs, prev, tgt, mask = _small_problem(2)
-    dims = (16, 16, 8)
+    nx, ny, nz, nb = 32, 32, 16, 2
+    rng = np.random.default_rng(2)
+    rhs = rng.normal(size=(nb, nz, ny, nx)).astype(np.float32)
+    prev = rng.normal(size=(nb, nz, ny, nx)).astype(np.float32)
+    tgt = (0.01 * rhs + 0.001 * rng.normal(size=(nb, nz, ny, nx))).astype(np.float32)
+    mask = (rng.random((nz, ny, nx)) < 0.05).astype(np.uint8)
     d = [bbpp.DeviceArray.from_host(a) for a in (rhs, prev, tgt, mask)]
-    h2 = 1.0 / 256.0
+    dims, h2 = (nx, ny, nz), 1.0 / 1024.0
     _, g = net.loss_grad(dims, h2, *d)
     off = sum(27 * ci * co + co for ci, co in NO.LAYERS[:layer])
     ci, co = NO.LAYERS[layer]
     n = 27 * ci * co + co
-    rng = np.random.default_rng(100 + layer)
     v = np.zeros_like(p)
-    rms = float(np.sqrt(np.mean(p[off:off + n] ** 2)))
-    v[off:off + n] = rng.normal(size=n).astype(np.float32) * rms
-    eps = 1e-2
-    net.set_params(p + eps * v)
-    lp, _ = net.loss_grad(dims, h2, *d, grads=False)
-    net.set_params(p - eps * v)
-    lm, _ = net.loss_grad(dims, h2, *d, grads=False)
+    v[off:off + n] = p[off:off + n]
+    ts = np.linspace(-0.05, 0.05, 41)
+    losses = []
+    for t in ts:
+        net.set_params(p + t * v)
+        losses.append(net.loss_grad(dims, h2, *d, grads=False)[0])
     net.set_params(p)
-    fd = (lp - lm) / (2 * eps)
+    slope = float(np.polyfit(ts, losses, 3)[2])
     an = float(np.dot(g.astype(np.float64), v.astype(np.float64)))
-    print("layer %d: finite difference %.6e, gradient %.6e" % (layer, fd, an))
-    assert abs(fd - an) <= 0.05 * abs(an), (fd, an)
+    print("layer %d: fitted slope %.6e, gradient %.6e" % (layer, slope, an))
+    assert abs(slope - an) <= 0.15 * abs(an), (slope, an)
 
 
 def test_net_training_lowers_loss(bbpp_lib):
@@ -302,7 +308,8 @@ def test_coarse_guess_matches_restatement(bbpp_lib, bc):
 
 def test_learned_guess_gain(bbpp_lib):
     """Train on an OU sequence at 32^3 and compare PCG iterations on held-out
-    steps: zero guess (the reference), warm start from p_prev, learned."""
+    steps: zero guess (the reference), warm start from p_prev, learned.  The
+    learned guess must beat the warm start it starts from, not only zero."""
     data, g, geom = learned.make_ou_dataset(32, 160, nsph=16, rad=2.0, seed=11, tol=1e-10)
     net = learned.Net(seed=1)
     hist = net.train(data, steps=600, batch=4, lr=2e-3)
@@ -320,7 +327,7 @@ def test_learned_guess_gain(bbpp_lib):
             res[key].append(out[key][0])
     z, w, l = (np.mean(res[k]) for k in ("zero", "warm", "learned"))
     print("iterations zero %.1f warm %.1f learned %.1f" % (z, w, l))
-    assert l < z  # the trained guess saves PCG iterations over the zero guess
+    assert l < w < z  # the trained guess saves PCG iterations over the warm start, which saves over zero
 
 
 @pytest.mark.parametrize("coarsen", [1, 2])

@@ -168,11 +168,16 @@ def test_fp32_ir_reaches_tolerance(lib, orc, name, n, tol, ir_mode):
     assert rep.status == bbpp.CONVERGED and rep.true_rel <= tol * 1.01
     assert rep.outer >= 1  # refinement sweeps, or reliable updates (the confirmation is one)
     xo, res = orc.pcg(to_orc(orc, g), rhs, mask, tol=1e-13)
+    # what the reference's method gives at the same tolerance: plain FP64 PCG
+    x64, _ = s.solve_host(rhs, mask, tol=tol, precision=bbpp.FP64)
     if mask is None:
-        x, xo = x - x.mean(), xo - xo.mean()
+        x, xo, x64 = x - x.mean(), xo - xo.mean(), x64 - x64.mean()
     err = np.abs(x - xo).max() / np.abs(xo).max()
-    # the solution error is bounded by the residual times the condition number
-    assert err < 1e4 * tol, err
+    err64 = np.abs(x64 - xo).max() / np.abs(xo).max()
+    # FP32 iterations with FP64 reliable updates lose no accuracy against the
+    # FP64 method at the same tolerance (a factor 10 for the different
+    # iterates; the floor, 100 tol, is far below the condition-number bound)
+    assert err < max(10 * err64, 100 * tol), (err, err64)
 
 
 @pytest.mark.parametrize("name,n,bc", [("C3", 64, None), ("C2", 48, None), ("C1", 32, None), ("C3", 64, "nnn")])
@@ -255,16 +260,23 @@ def test_solve_odd_shapes(lib, orc, dims, bc, precision, ir_mode):
         # is defined up to a constant, which FP32 round-off may shift
         x, xo = x - x.mean(), xo - xo.mean()
     err = np.abs(x - xo).max() / max(np.abs(xo).max(), 1e-300)
-    assert err < 1e4 * tol, err
+    # against the FP64 method at the same tolerance, as in test_fp32_ir_reaches_tolerance
+    x64, _ = s.solve_host(b, mask, tol=tol, precision=bbpp.FP64)
+    if not mask.any():
+        x64 = x64 - x64.mean()
+    err64 = np.abs(x64 - xo).max() / max(np.abs(xo).max(), 1e-300)
+    assert err < max(10 * err64, 100 * tol), (err, err64)
 
 
 @pytest.mark.parametrize("name,n,bc", [("C3", 128, None), ("C1", 64, None), ("C2", 64, "nnn")])
 @pytest.mark.parametrize("ws_ns", ["3", "4", "6"])
-def test_ws_fused_kernel_bit_identical(lib, name, n, bc, ws_ns, monkeypatch):
-    """The warp-specialised fused kernel (producer warp, empty barriers, lower
-    z neighbour from a register) against the fused kernel it replaces, chosen
-    per context when it is created: the same iterations and a bit-identical
-    solution, for ring depths of 3, 4 and 6 stages."""
+def test_ws_fused_kernel_matches_fused(lib, name, n, bc, ws_ns, monkeypatch):
+    """The warp-specialised fused kernel (producer warp, empty barriers, x and
+    mask staged by tensor copies, lower z neighbour from a register) against the
+    fused kernel, chosen per context when it is created, for ring depths of 3,
+    4 and 6 stages.  Per cell both compute the same values; the two launches may
+    cut z into different chunks, so the dot products sum their CTA partials in a
+    different grouping, and the iterates agree to rounding, not bit for bit."""
     g, mask, rhs, _ = problems.make_problem(name, n=n)
     if bc is not None:
         g = problems.make_grid(n, bc)
@@ -276,5 +288,7 @@ def test_ws_fused_kernel_bit_identical(lib, name, n, bc, ws_ns, monkeypatch):
     x0, r0 = s_old.solve_host(rhs, mask, tol=1e-8, precision=bbpp.FP32_IR)
     x1, r1 = s_ws.solve_host(rhs, mask, tol=1e-8, precision=bbpp.FP32_IR)
     assert r0.status == r1.status == bbpp.CONVERGED
-    assert r0.iters == r1.iters and r0.outer == r1.outer
-    assert np.array_equal(x0, x1)
+    assert abs(r0.iters - r1.iters) <= 1 and r1.true_rel <= 1e-8 * 1.01
+    if mask is None:
+        x0, x1 = x0 - x0.mean(), x1 - x1.mean()
+    assert np.abs(x0 - x1).max() <= 1e-5 * np.abs(x0).max()
