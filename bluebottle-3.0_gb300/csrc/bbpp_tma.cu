@@ -129,7 +129,7 @@ struct TmaMaps {
 
 // Load rows [y, y + nrow) of plane z of one array into dst (row-major, nx
 // floats per row).  4-D maps split x into 256-wide pieces (nx > 256).
-__device__ __forceinline__ void load_rows(void *dst, const CUtensorMap *map, unsigned long long *bar, int y, int z,
+__device__ __forceinline__ void load_rows(float *dst, const CUtensorMap *map, unsigned long long *bar, int y, int z,
                                           bool four_d, unsigned long long pol) {
   if (four_d) tma_load_4d(dst, map, bar, 0, 0, y, z, pol);
   else tma_load_3d(dst, map, bar, 0, y, z, pol);
@@ -406,7 +406,6 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
 // halo rows are another CTA's own cells.
 struct FusedMaps {
   CUtensorMap r_rows, r_row, a_rows, a_row, p_rows, p_row;
-  CUtensorMap x_rows, m_rows;  // the slab rows of x and of the mask (bytes): the warp-specialised kernel stages them
 };
 
 template <int NPT, bool MASK, bool ISO>
@@ -721,9 +720,7 @@ __global__ void __launch_bounds__(TNT) k1_fused(const GeoL G, const __grid_const
 // neighbour from the centre value the same thread read for plane j - 1 (a
 // register), so a stage is free once the stencil of its own plane is done:
 // with ns stages, plane j + ns is in flight from the end of plane j's stencil,
-// ns - 2 planes ahead of the prep that waits for it.  The producer also stages
-// the slab rows of x and of the mask of every own plane, so the compute warps
-// issue no global load at all.  The compute warps still
+// ns - 2 planes ahead of the prep that waits for it.  The compute warps still
 // meet at a barrier of their own once per plane, between the prep of plane
 // j + 1 (rows other threads read) and the stencil of plane j.
 // Arithmetic, order of the partial sums and the stored values are those of
@@ -775,18 +772,13 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
   const int nxv = nx >> 2;
   const int rows = ty + 2;
   const int arr = rows * nx;
-  // stage q: r, Ap_old -> p_new, p_old ([3][rows][nx]) and the own rows of x
-  // ([ty][nx]); then the own rows of the mask, [ns][ty][nx] bytes
-  const int sstride = 3 * arr + ty * nx;
-  float *stage = reinterpret_cast<float *>(smem_raw);
-  uint8_t *mstage = reinterpret_cast<uint8_t *>(stage + (size_t)ns * sstride);
+  float *stage = reinterpret_cast<float *>(smem_raw);  // [ns][3][rows][nx]: r, Ap_old -> p_new, p_old
   const int y0 = blockIdx.x * ty;
   const int z0 = blockIdx.y * kz, z1 = min(z0 + kz, nz);
   const int np = z1 - z0 + 2;
   const int nj = z1 - z0;
   const unsigned int plane = (unsigned int)nx * (unsigned int)ny;
   const unsigned int tx_bytes = (unsigned int)((1 + (lag ? 1 : 0) + (first ? 0 : 1)) * arr * 4);
-  const unsigned int own_bytes = (unsigned int)((lag ? ty * nx * 4 : 0) + (MASK ? ty * nx : 0));
   const int ys = G.py ? (y0 - 1 + ny) % ny : y0 - 1;
   const int yn = G.py ? (y0 + ty) % ny : y0 + ty;
 
@@ -832,12 +824,9 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
       if (lane == 0 && !(skip_one && j == 2)) {
         int zr = z0 - 1 + j;
         if (G.pz) zr = (zr + nz) % nz;
-        float *rs = stage + (size_t)q * sstride;
+        float *rs = stage + (size_t)q * 3 * arr;
         unsigned long long *bar = &s_full[q];
-        const bool own = j >= 1 && j <= nj;  // a plane of this chunk (not a halo plane)
-        mbar_expect_tx(bar, tx_bytes + (own ? own_bytes : 0u));
-        if (own && lag) load_rows(rs + 3 * arr, &M.x_rows, bar, y0, zr, four_d, pol_stream);
-        if (own && MASK) load_rows(mstage + (size_t)q * ty * nx, &M.m_rows, bar, y0, zr, four_d, pol_mask);
+        mbar_expect_tx(bar, tx_bytes);
         load_rows(rs + nx, &M.r_rows, bar, y0, zr, four_d, pol_n);
         load_rows(rs, &M.r_row, bar, ys, zr, four_d, pol_n);
         load_rows(rs + (ty + 1) * nx, &M.r_row, bar, yn, zr, four_d, pol_n);
@@ -872,7 +861,7 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
     auto prep = [&](int j) {
       const int q = j % ns;
       if (!wait_phase(&s_full[q], (unsigned int)(j / ns) & 1u, limit)) bad = true;
-      float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)q * sstride);
+      float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)q * 3 * arr);
       float4 *as = rs + arr / 4;
       const float4 *ps = rs + 2 * (arr / 4);
       const int zr = z0 - 1 + j;
@@ -939,15 +928,28 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
       orow[k] = e / nxv;
       oc4[k] = e - orow[k] * nxv;
     }
+    uchar4 mkA[NPT], mkB[NPT];
+    float4 xvA[NPT], xvB[NPT];
     float4 bv[NPT];  // p_new of the plane below, own cells
-    auto stencil = [&](int j) {
+    auto fetch = [&](int zc, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
+#pragma unroll
+      for (int k = 0; k < NPT; k++) {
+        const unsigned int c =
+            plane * (unsigned int)zc + (unsigned int)nx * (unsigned int)(y0 + orow[k]) + 4u * oc4[k];
+        if (MASK) {
+          const unsigned int m = ld_u32_pol(mask + c, pol_mask);
+          mk[k] = make_uchar4(m & 0xffu, (m >> 8) & 0xffu, (m >> 16) & 0xffu, m >> 24);
+        }
+        if (lag) xv[k] = ld4_pol(reinterpret_cast<const float4 *>(x + c), pol_stream);
+      }
+    };
+
+    auto stencil = [&](int j, const uchar4 (&mk)[NPT], const float4 (&xv)[NPT]) {
       const int zc = z0 - 1 + j;
-      const float *cr = stage + (size_t)(j % ns) * sstride;        // r_new, plane z
+      const float *cr = stage + (size_t)(j % ns) * 3 * arr;       // r_new, plane z
       const float *cs = cr + arr;                                  // p_new, plane z
-      const float *ts = stage + (size_t)((j + 1) % ns) * sstride + arr;
+      const float *ts = stage + (size_t)((j + 1) % ns) * 3 * arr + arr;
       const float *po = cr + 2 * arr;                              // p_old, plane z
-      const float *xs = cr + 3 * arr;                              // x, own rows of plane z
-      const uint8_t *ms = mstage + (size_t)(j % ns) * ty * nx;     // mask, own rows of plane z
       const int wz = 9 * wall_count(zc, nz, G.pz);
       const bool interior = G.px && G.py && wz == 0;
 #pragma unroll
@@ -958,7 +960,8 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
         const float4 n = *reinterpret_cast<const float4 *>(cs + off + nx);
         const float4 s = *reinterpret_cast<const float4 *>(cs + off - nx);
         const float4 t = *reinterpret_cast<const float4 *>(ts + off);
-        const float4 b = j == 1 ? *reinterpret_cast<const float4 *>(stage + (size_t)((j - 1) % ns) * sstride + arr + off)
+        const float4 b = j == 1 ? *reinterpret_cast<const float4 *>(stage + (size_t)((j - 1) % ns) * 3 * arr + arr +
+                                                                     off)
                                 : bv[k];
         bv[k] = c;
         float w = __shfl_up_sync(0xffffffffu, c.w, 1);
@@ -989,11 +992,10 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
           a[3] = apply_L<float, ISO>(G, s_dL, cls[3], c.w, ea, c.z, n.w, s.w, t.w, b.w);
         }
         if (MASK) {
-          const uchar4 mk = *reinterpret_cast<const uchar4 *>(ms + row * nx + 4 * c4);
-          if (mk.x) a[0] = 0.f;
-          if (mk.y) a[1] = 0.f;
-          if (mk.z) a[2] = 0.f;
-          if (mk.w) a[3] = 0.f;
+          if (mk[k].x) a[0] = 0.f;
+          if (mk[k].y) a[1] = 0.f;
+          if (mk[k].z) a[2] = 0.f;
+          if (mk[k].w) a[3] = 0.f;
         }
         const float4 r = *reinterpret_cast<const float4 *>(cr + off);
         const float rv[4] = {r.x, r.y, r.z, r.w};
@@ -1018,7 +1020,7 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
         st4_pol(reinterpret_cast<float4 *>(rout + g), r, pol_n);
         if (lag) {
           const float4 q = *reinterpret_cast<const float4 *>(po + off);
-          float4 xo = *reinterpret_cast<const float4 *>(xs + row * nx + 4 * c4);
+          float4 xo = xv[k];
           xo.x = fmaf(alpha, q.x, xo.x);
           xo.y = fmaf(alpha, q.y, xo.y);
           xo.z = fmaf(alpha, q.z, xo.z);
@@ -1033,15 +1035,22 @@ __global__ void __launch_bounds__(WS_THREADS, 3) k1_fused_ws(const GeoL G, const
       if (lane == 0) mbar_arrive(&s_empty[j % ns]);
     };
 
+    fetch(z0, mkA, xvA);
+    if (nj >= 2) fetch(z0 + 1, mkB, xvB);
     prep(0);
     prep(1);
-    for (int j = 1; j <= nj; j++) {
+    auto step = [&](int j, uchar4 (&mk)[NPT], float4 (&xv)[NPT]) {
       prep(j + 1);
       fence_proxy_async();  // this thread's stage writes before later tensor copies into the stage
       compute_sync();
-      stencil(j);
+      stencil(j, mk, xv);
       if (j == 1) release(0);
       release(j);
+      if (j + 2 <= nj) fetch(z0 + j + 1, mk, xv);
+    };
+    for (int j = 1; j <= nj; j += 2) {
+      step(j, mkA, xvA);
+      if (j + 1 <= nj) step(j + 1, mkB, xvB);
     }
   }
 
@@ -1097,27 +1106,26 @@ EncodeTiled encode_fn() {
   return fn;
 }
 
-// map of an nx x ny x nz array (FP32, or bytes with esize 1) with boxes of
-// nrow full rows
-bool make_map(CUtensorMap *m, const void *base, int nx, int ny, int nz, int nrow, int esize = 4) {
+// map of an nx x ny x nz float array with boxes of nrow full rows
+bool make_map(CUtensorMap *m, const float *base, int nx, int ny, int nz, int nrow) {
   EncodeTiled fn = encode_fn();
   if (!fn) return false;
   CUresult r;
   const cuuint32_t es[4] = {1, 1, 1, 1};
-  const CUtensorMapDataType dt = esize == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-  const cuuint64_t e = (cuuint64_t)esize;
   if (nx <= 256) {
     const cuuint64_t dim[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-    const cuuint64_t str[2] = {(cuuint64_t)nx * e, (cuuint64_t)nx * ny * e};
+    const cuuint64_t str[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
     const cuuint32_t box[3] = {(cuuint32_t)nx, (cuuint32_t)nrow, 1};
-    r = fn(m, dt, 3, const_cast<void *>(base), dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dim, str, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   } else {  // x split into 256-wide pieces so a box still lands as whole rows
     const cuuint64_t dim[4] = {256, (cuuint64_t)(nx / 256), (cuuint64_t)ny, (cuuint64_t)nz};
-    const cuuint64_t str[3] = {256 * e, (cuuint64_t)nx * e, (cuuint64_t)nx * ny * e};
+    const cuuint64_t str[3] = {1024, (cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
     const cuuint32_t box[4] = {256, (cuuint32_t)(nx / 256), (cuuint32_t)nrow, 1};
-    r = fn(m, dt, 4, const_cast<void *>(base), dim, str, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float *>(base), dim, str, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   }
   return r == CUDA_SUCCESS;
 }
@@ -1162,13 +1170,6 @@ struct bbpp_tma_state {
   int wns = 0, wkz = 0, wsmem = 0;
   dim3 wgrid;
   std::vector<MapPair> maps;
-  // slab-row maps of x and the mask (FP32 or bytes), for the warp-specialised kernel
-  struct RowsMap {
-    const void *ptr;
-    int esize;
-    CUtensorMap map;
-  };
-  std::vector<RowsMap> rmaps;
 };
 
 // Decide whether the grid suits the TMA kernel and pick its launch shape.
@@ -1264,10 +1265,8 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
   // is done, so 3 stages already keep one plane in flight (BBPP_WS_NS, 3..8)
   if (t->fok && env_int("BBPP_FUSED_WS", 0)) {
     int wns = std::max(3, std::min(8, env_int("BBPP_WS_NS", 4)));
-    // a stage: r, Ap_old, p_old with halo rows, the own rows of x, and of the mask (bytes)
-    const int wstage = (3 * (ty + 2) * nx + ty * nx) * 4 + ty * nx;
-    while (wns > 3 && wns * wstage > kMaxStageBytes) wns--;
-    const int wsmem = wns * wstage;
+    while (wns > 3 && wns * 3 * (ty + 2) * nx * 4 > kMaxStageBytes) wns--;
+    const int wsmem = wns * 3 * (ty + 2) * nx * 4;
     int wper = 0;
     if (wsmem <= kMaxStageBytes) {
 #define BBPP_WS_OCC(N) \
@@ -1327,23 +1326,6 @@ static bool get_maps(bbpp_tma_state *t, const float *p, const GeoL &G, MapPair *
   return true;
 }
 
-// the ty-row map of one array (FP32 x, or the byte mask)
-static bool get_rows_map(bbpp_tma_state *t, const void *p, int esize, const GeoL &G, CUtensorMap *out) {
-  for (const auto &m : t->rmaps)
-    if (m.ptr == p && m.esize == esize) {
-      *out = m.map;
-      return true;
-    }
-  bbpp_tma_state::RowsMap m;
-  m.ptr = p;
-  m.esize = esize;
-  if (!make_map(&m.map, p, G.nx, G.ny, G.nz, t->ty, esize)) return false;
-  if (t->rmaps.size() >= 8) t->rmaps.erase(t->rmaps.begin());
-  t->rmaps.push_back(m);
-  *out = m.map;
-  return true;
-}
-
 // tensor maps of the six buffers of a fused solve, built before its graphs
 bool bbpp_tma_fused_maps(bbpp_ctx *ctx, const float *const r[2], const float *const a[2], const float *const p[2]) {
   bbpp_tma_state *t = ctx->tma;
@@ -1369,10 +1351,6 @@ bool bbpp_tma_fused(bbpp_ctx *ctx, const uint8_t *mask, const float *rin, const 
   M.a_row = ma.row;
   M.p_rows = mp.rows;
   M.p_row = mp.row;
-  if (t->wok) {
-    if (!get_rows_map(t, x, 4, ctx->GL, &M.x_rows)) return false;
-    if (mask && !get_rows_map(t, mask, 1, ctx->GL, &M.m_rows)) return false;
-  }
 #define BBPP_FUSED_LAUNCH(N, MK, IS)                                                                              \
   if (t->wok)                                                                                                     \
     bbpp_launch(ctx, k1_fused_ws<N, MK, IS>, t->wgrid, dim3(WS_THREADS), (size_t)t->wsmem, ctx->GL, M, rout, pnew, \

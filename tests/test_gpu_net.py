@@ -187,10 +187,11 @@ def test_net_gradient_finite_differences(bbpp_lib, layer):
     weights measures rounding, not slope.  The check therefore moves a whole
     layer along its own weights, w -> (1 + t) w (and its bias), at 41 points
     t in [-0.05, 0.05], and takes the slope at t = 0 of a cubic fitted to the
-    losses, against g . w.  On the network oracle (FP32 with the same BF16
-    rounding) this estimate lands within 10% of its autograd slope for every
-    layer at this volume, so the bound is 15%: a layer gradient off in sign, by
-    a factor, or missing a term fails it."""
+    losses, against g . w.  The rounding leaves noise on the losses, so the bound
+    is 10% of |g . w| plus four standard errors of the fitted slope (from the
+    fit's residuals): a layer gradient off in sign, by a factor, or missing a
+    term fails it, while a layer whose slope is small next to the noise does
+    not fail on rounding alone."""
     net = learned.Net(seed=3)
     p = net.get_params()
     nx, ny, nz, nb = 32, 32, 16, 2
@@ -213,10 +214,12 @@ def test_net_gradient_finite_differences(bbpp_lib, layer):
         net.set_params(p + t * v)
         losses.append(net.loss_grad(dims, h2, *d, grads=False)[0])
     net.set_params(p)
-    slope = float(np.polyfit(ts, losses, 3)[2])
+    coef, cov = np.polyfit(ts, losses, 3, cov=True)
+    slope, se = float(coef[2]), float(np.sqrt(cov[2, 2]))
     an = float(np.dot(g.astype(np.float64), v.astype(np.float64)))
-    print("layer %d: fitted slope %.6e, gradient %.6e" % (layer, slope, an))
-    assert abs(slope - an) <= 0.15 * abs(an), (slope, an)
+    print("layer %d: fitted slope %.6e +- %.1e, gradient %.6e" % (layer, slope, se, an))
+    assert abs(slope - an) <= 0.1 * abs(an) + 4 * se, (slope, se, an)
+    assert se < abs(an)  # the fit resolves the slope: the check is not vacuous
 
 
 def test_net_training_lowers_loss(bbpp_lib):

@@ -271,8 +271,8 @@ def test_solve_odd_shapes(lib, orc, dims, bc, precision, ir_mode):
 @pytest.mark.parametrize("name,n,bc", [("C3", 128, None), ("C1", 64, None), ("C2", 64, "nnn")])
 @pytest.mark.parametrize("ws_ns", ["3", "4", "6"])
 def test_ws_fused_kernel_matches_fused(lib, name, n, bc, ws_ns, monkeypatch):
-    """The warp-specialised fused kernel (producer warp, empty barriers, x and
-    mask staged by tensor copies, lower z neighbour from a register) against the
+    """The warp-specialised fused kernel (producer warp, empty barriers, lower
+    z neighbour from a register) against the
     fused kernel, chosen per context when it is created, for ring depths of 3,
     4 and 6 stages.  Per cell both compute the same values; the two launches may
     cut z into different chunks, so the dot products sum their CTA partials in a
