@@ -208,7 +208,9 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   // p_new over a stage, in place of r
   auto prep = [&](int j) {
     const int s = j % ns;
-    if (!mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u, limit)) bad = true;
+    // after a wait has run out this thread waits no more: the copy unit is
+    // behind, and the drain at the end waits for what is in flight
+    if (!bad && !mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u, limit)) bad = true;
     float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)s * 2 * arr);
     const float4 *ps = reinterpret_cast<const float4 *>(stage + (size_t)s * 2 * arr + arr);
     int zr = z0 - 1 + j;
@@ -369,7 +371,10 @@ __global__ void __launch_bounds__(TNT) k1_tma(const GeoL G, const __grid_constan
   if (__syncthreads_or(bad)) {
     // drain: every stage's last issued copy, with bounded waits
     if (tid == 0) {
-      for (int j = max(0, np - ns); j < np; j++) mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u, limit);
+      // the last copy into every stage, with ten times the bound: the CTA must
+      // not exit while a copy into its shared memory is still in flight
+      for (int j = max(0, np - ns); j < np; j++)
+        mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u, 10ull * limit);
       atomicExch(&st->done, (int)DONE_TIMEOUT);
     }
     return;
@@ -491,7 +496,9 @@ __global__ void __launch_bounds__(TNT) k1_fused(const GeoL G, const __grid_const
   // over a stage: r -= alpha Ap_old in place, p_new into the Ap_old slot
   auto prep = [&](int j) {
     const int s = j % ns;
-    if (!mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u, limit)) bad = true;
+    // after a wait has run out this thread waits no more: the copy unit is
+    // behind, and the drain at the end waits for what is in flight
+    if (!bad && !mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u, limit)) bad = true;
     float4 *rs = reinterpret_cast<float4 *>(stage + (size_t)s * 3 * arr);
     float4 *as = rs + arr / 4;
     const float4 *ps = rs + 2 * (arr / 4);
@@ -683,7 +690,10 @@ __global__ void __launch_bounds__(TNT) k1_fused(const GeoL G, const __grid_const
 
   if (__syncthreads_or(bad)) {
     if (tid == 0) {
-      for (int j = max(0, np - ns); j < np; j++) mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u, limit);
+      // the last copy into every stage, with ten times the bound: the CTA must
+      // not exit while a copy into its shared memory is still in flight
+      for (int j = max(0, np - ns); j < np; j++)
+        mbar_wait(&s_full[j % ns], (unsigned int)(j / ns) & 1u, 10ull * limit);
       atomicExch(&st->done, (int)DONE_TIMEOUT);
     }
     return;

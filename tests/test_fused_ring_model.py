@@ -78,7 +78,7 @@ def test_model_matches_kernel_source():
     assert "if (tid == 0 && j >= 2 && j - 2 + ns < np) issue(j - 2 + ns);" in body
     assert "mbar_wait(&s_full[s], (unsigned int)(j / ns) & 1u, limit)" in body
     assert "const int pre = min(ns, np);" in body
-    assert re.search(r"for \(int j = max\(0, np - ns\); j < np; j\+\+\) mbar_wait", body)
+    assert re.search(r"for \(int j = max\(0, np - ns\); j < np; j\+\+\)\s+mbar_wait", body)
     # the host keeps the ring at 4..8 stages
     assert "ns = std::max(4, std::min(8, ns));" in src
 
