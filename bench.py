@@ -452,11 +452,16 @@ def run_ours(args):
         kname, nl, kms, kbytes = top
         achieved = (kbytes / nl) / (kms / nl * 1e-3) / 1e9
         tot = sum(k[2] for k in ks)
-        return {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hb, "unit": "GB/s",
-                "frac": achieved / hb, "traffic": NCU_TRAFFIC.get(kname), "algorithmic_bytes": kbytes / nl,
-                "launches": nl, "avg_us": kms / nl * 1e3,
-                "share": kms / tot if tot else None,
-                "peak_source": "measured" if "fallback" not in pk else "fallback"}
+        out = {"kernel": kname, "bound": "hbm", "achieved": achieved, "peak": hb, "unit": "GB/s",
+               "frac": achieved / hb, "traffic": NCU_TRAFFIC.get(kname), "algorithmic_bytes": kbytes / nl,
+               "launches": nl, "avg_us": kms / nl * 1e3,
+               "share": kms / tot if tot else None,
+               "peak_source": "measured" if "fallback" not in pk else "fallback"}
+        if kname == "fused_f32" and stream_gbs:
+            # what a plain streaming kernel with the same per-cell traffic reaches on this GPU
+            out["stream_same_mix_gbs"] = stream_gbs
+            out["frac_of_stream_same_mix"] = achieved / stream_gbs
+        return out
 
     def fp64_roof(name):
         """The plain FP64 solve against the FP64 pipe it is bound by: FP64 thread
@@ -477,9 +482,10 @@ def run_ours(args):
                 "frac": achieved / fma_rate, "inst_per_cell": {k: v for k, v in NCU_FP64_INST.items()},
                 "kernels_ms_share": ms / sum(k[2] for k in ks), "peak_source": "bbpp_fp64_fma_rate (this run)"}
 
-    fma_rate = None
+    fma_rate = stream_gbs = None
     try:
         fma_rate = bbpp.fp64_fma_rate()
+        stream_gbs = bbpp.stream_mix_rate(N) / 1e9
     except Exception:  # noqa: BLE001
         pass
     H = res[headline]

@@ -124,6 +124,7 @@ def lib():
         "bbpp_sync": (I, []),
         "bbpp_flush_l2": (I, []),
         "bbpp_fp64_fma_rate": (I, [ctypes.POINTER(D)]),
+        "bbpp_stream_mix_rate": (I, [ctypes.c_longlong, ctypes.POINTER(D)]),
         "bbpp_host_alloc": (I, [S, ctypes.POINTER(P)]),
         "bbpp_host_free": (I, [P]),
         "bbpp_kernel_stats": (I, [P, P, I, ctypes.POINTER(I)]),
@@ -364,6 +365,14 @@ def rng_gauss(seed, n):
 
 def flush_l2():
     _check(lib().bbpp_flush_l2())
+
+
+def stream_mix_rate(cells):
+    """Bytes/s of a streaming kernel with the fused iteration's per-cell traffic
+    (bbpp_stream_mix_rate)."""
+    v = ctypes.c_double()
+    _check(lib().bbpp_stream_mix_rate(int(cells), ctypes.byref(v)))
+    return v.value
 
 
 def fp64_fma_rate():

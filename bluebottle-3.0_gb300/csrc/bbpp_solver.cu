@@ -1314,6 +1314,74 @@ extern "C" int bbpp_fp64_fma_rate(double *fma_per_s) {
   return 0;
 }
 
+// The bandwidth a plain streaming kernel reaches with the fused FP32
+// iteration's per-cell traffic: four FP32 reads, one mask byte, four FP32
+// writes (33 B/cell), elementwise, no stencil.  It separates what the traffic
+// mix allows from what the stencil's pipeline costs.
+__global__ void __launch_bounds__(256) k_stream_mix(const float4 *__restrict__ r, const float4 *__restrict__ a,
+                                                    const float4 *__restrict__ p, const float4 *__restrict__ x,
+                                                    const uchar4 *__restrict__ m, float4 *__restrict__ ro,
+                                                    float4 *__restrict__ po, float4 *__restrict__ ao,
+                                                    float4 *__restrict__ xo, long long n4) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+    float4 rv = r[i], av = a[i], pv = p[i], xv = x[i];
+    const uchar4 mv = m[i];
+    const float s = mv.x | mv.y | mv.z | mv.w ? 0.f : 1.f;
+    rv.x = fmaf(-0.5f, av.x, rv.x);
+    rv.y = fmaf(-0.5f, av.y, rv.y);
+    rv.z = fmaf(-0.5f, av.z, rv.z);
+    rv.w = fmaf(-0.5f, av.w, rv.w);
+    pv.x = fmaf(0.5f * s, pv.x, rv.x);
+    pv.y = fmaf(0.5f, pv.y, rv.y);
+    pv.z = fmaf(0.5f, pv.z, rv.z);
+    pv.w = fmaf(0.5f, pv.w, rv.w);
+    xv.x += pv.x;
+    xv.y += pv.y;
+    xv.z += pv.z;
+    xv.w += pv.w;
+    ro[i] = rv;
+    po[i] = pv;
+    ao[i] = av;
+    xo[i] = xv;
+  }
+}
+
+extern "C" int bbpp_stream_mix_rate(long long cells, double *bytes_per_s) {
+  bbpp_ctx *ctx = nullptr;
+  if (!bytes_per_s || cells < 1024 || cells % 4) return BBPP_BAD_ARG;
+  float *buf = nullptr;
+  unsigned char *m = nullptr;
+  cudaEvent_t e0, e1;
+  CK(cudaMalloc(&buf, sizeof(float) * 8 * (size_t)cells));
+  CK(cudaMalloc(&m, (size_t)cells));
+  CK(cudaMemset(buf, 0, sizeof(float) * 8 * (size_t)cells));
+  CK(cudaMemset(m, 0, (size_t)cells));
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const long long n = cells, n4 = cells / 4;
+  const int blocks = 16 * dev_sms();
+  float best = 0.f;
+  for (int rep = 0; rep < 6; rep++) {
+    const int rc = bbpp_flush_l2();
+    if (rc) return rc;
+    CK(cudaEventRecord(e0));
+    k_stream_mix<<<blocks, 256>>>((const float4 *)buf, (const float4 *)(buf + n), (const float4 *)(buf + 2 * n),
+                                  (const float4 *)(buf + 3 * n), (const uchar4 *)m, (float4 *)(buf + 4 * n),
+                                  (float4 *)(buf + 5 * n), (float4 *)(buf + 6 * n), (float4 *)(buf + 7 * n), n4);
+    CK(cudaEventRecord(e1));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep >= 1 && (best == 0.f || ms < best)) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  cudaFree(m);
+  *bytes_per_s = 33.0 * (double)cells / (best * 1e-3);
+  return 0;
+}
+
 // ----------------------------------------------------------- kernel stats --
 static const char *kk_name[KK_COUNT] = {"search_spmv", "update", "axpy_x", "resid", "search_spmv_f32",
                                         "update_f32", "axpy_x_f32", "resid_f32", "fused_f32"};

@@ -195,6 +195,12 @@ int bbpp_flush_l2(void);
  * plain FP64 solve's roofline is reported against.  No counterpart in the
  * reference. */
 int bbpp_fp64_fma_rate(double *fma_per_s);
+/* Bytes per second a plain streaming kernel reaches with the fused FP32
+ * iteration's per-cell traffic over `cells` cells (four FP32 reads, one mask
+ * byte, four FP32 writes: 33 B/cell; L2 flushed before each of five timed
+ * launches, the best kept).  Allocates its buffers (about 33 B per cell) for
+ * the measurement.  No counterpart in the reference. */
+int bbpp_stream_mix_rate(long long cells, double *bytes_per_s);
 /* Page-locked host memory (for end-to-end timing from pinned buffers). */
 int bbpp_host_alloc(size_t bytes, void **ptr);
 int bbpp_host_free(void *ptr);
