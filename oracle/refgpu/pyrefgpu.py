@@ -12,6 +12,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(os.path.dirname(HERE), "_ref")
 CUBIN = os.path.join(REF_DIR, "ref_solver.cubin")
+CAGES_CUBIN = os.path.join(REF_DIR, "ref_cages.cubin")
 LIB = os.path.join(REF_DIR, "librefgpu.so")
 _lib = None
 
@@ -21,7 +22,8 @@ def build_host(quiet=True):
     if not os.path.exists(CUBIN):
         return None
     cmd = [os.environ.get("NVCC", "nvcc"), "-shared", "-Xcompiler", "-fPIC", "-O2", "-std=c++17",
-           "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB, os.path.join(HERE, "ref_gpu.cu")]
+           "-gencode", "arch=compute_103a,code=sm_103a", "-o", LIB, os.path.join(HERE, "ref_gpu.cu"),
+           os.path.join(HERE, "ref_cages.cu")]
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
     return LIB
 
@@ -39,6 +41,16 @@ def lib():
         L.refgpu_setup.argtypes = [I, I, I, D, D, D, P, P]
         L.refgpu_solve.argtypes = [P, D, I, P, ctypes.POINTER(I), ctypes.POINTER(D), ctypes.POINTER(D)]
         L.refgpu_error.restype = ctypes.c_char_p
+        L.refgpu_cages_set_cubin.argtypes = [P, ctypes.c_size_t]
+        L.refgpu_cages_setup.argtypes = [I, I, I, D, D, D, P]
+        L.refgpu_cages_sizes.argtypes = [P]
+        L.refgpu_build_cages.argtypes = [I, I, P, P, P, P, P, P, ctypes.POINTER(D)]
+        L.refgpu_cages_error.restype = ctypes.c_char_p
+        if os.path.exists(CAGES_CUBIN):
+            cdata = open(CAGES_CUBIN, "rb").read()
+            cbuf = ctypes.create_string_buffer(cdata, len(cdata))
+            L._cages_cubin = cbuf
+            L.refgpu_cages_set_cubin(cbuf, len(cdata))
         data = open(CUBIN, "rb").read()
         buf = ctypes.create_string_buffer(data, len(data))
         L._cubin = buf
@@ -77,3 +89,51 @@ class RefSolver:
 
     def close(self):
         lib().refgpu_free()
+
+
+def cages_available():
+    return available() and os.path.exists(CAGES_CUBIN)
+
+
+class RefCages:
+    """The reference's cage builder (cuda_build_cages around its own kernels of
+    src/particle_kernel.cu) on one GPU for one grid (bc: W,E,S,N,B,T with 0
+    periodic / 2 Neumann)."""
+
+    def __init__(self, nx, ny, nz, dx, dy, dz, bc):
+        L = lib()
+        rc = L.refgpu_cages_setup(nx, ny, nz, dx, dy, dz, (ctypes.c_int * 6)(*bc))
+        if rc:
+            raise RuntimeError("refgpu_cages_setup %d: %s" % (rc, L.refgpu_cages_error().decode()))
+        sz = np.zeros(10, np.int64)
+        L.refgpu_cages_sizes(sz.ctypes.data)
+        self.sizes = [int(v) for v in sz[:4]]
+        self.part_bytes, self.off_n, self.off_r, self.off_x, self.off_y, self.off_z = (int(v) for v in sz[4:10])
+
+    def parts_bytes(self, xyzr):
+        """(n, 4) rows x, y, z, r -> the reference's part_struct array as bytes."""
+        xyzr = np.asarray(xyzr, np.float64).reshape(-1, 4)
+        raw = np.zeros((max(len(xyzr), 1), self.part_bytes), np.uint8)
+        for n, (x, y, z, r) in enumerate(xyzr):
+            raw[n, self.off_n:self.off_n + 4] = np.frombuffer(np.int32(n).tobytes(), np.uint8)
+            for off, v in ((self.off_r, r), (self.off_x, x), (self.off_y, y), (self.off_z, z)):
+                raw[n, off:off + 8] = np.frombuffer(np.float64(v).tobytes(), np.uint8)
+        return raw
+
+    def build(self, xyzr, with_parts=True):
+        """Returns (phase, phase_shell, flag_u, flag_v, flag_w, ms): the
+        reference's ghosted arrays (flat) and the device time of the builder."""
+        L = lib()
+        xyzr = np.asarray(xyzr, np.float64).reshape(-1, 4)
+        raw = np.ascontiguousarray(self.parts_bytes(xyzr))
+        out = [np.zeros(self.sizes[0], np.int32), np.zeros(self.sizes[0], np.int32),
+               np.zeros(self.sizes[1], np.int32), np.zeros(self.sizes[2], np.int32), np.zeros(self.sizes[3], np.int32)]
+        ms = ctypes.c_double()
+        rc = L.refgpu_build_cages(1 if with_parts else 0, len(xyzr), raw.ctypes.data, *[a.ctypes.data for a in out],
+                                  ctypes.byref(ms))
+        if rc:
+            raise RuntimeError("refgpu_build_cages %d: %s" % (rc, L.refgpu_cages_error().decode()))
+        return (*out, ms.value)
+
+    def close(self):
+        lib().refgpu_cages_free()

@@ -10,6 +10,7 @@ restated one-rank host loop of src/cuda_solver.cu.  These tests check:
     same iteration count (within one) and solutions within 1e-10 relative.
 Skipped when the cubin is absent (it is built where the reference tree is).
 """
+import ctypes
 import os
 import sys
 
@@ -101,3 +102,79 @@ def test_library_matches_reference_gpu_full_size(bbpp_lib, name, pp_residual):
     assert rep.true_rel <= 1e-11, rep.true_rel
     err = np.linalg.norm(x - phi) / np.linalg.norm(phi)
     assert err <= 1e-10, err
+
+
+def with_periodic_copies(cents, radii, box, bc):
+    """(x, y, z, r) rows of the particles plus, along periodic axes, the shifted
+    copy of every particle within two radii of a boundary: the list a one-rank
+    Bluebottle run hands its cage builder."""
+    rows = [list(c) + [r] for c, r in zip(cents, radii)]
+    out = list(rows)
+    for row in rows:
+        for a in range(3):
+            if bc[2 * a] == 0:
+                if row[a] < 2 * row[3]:
+                    cp = list(row)
+                    cp[a] += box[a]
+                    out.append(cp)
+                elif row[a] > box[a] - 2 * row[3]:
+                    cp = list(row)
+                    cp[a] -= box[a]
+                    out.append(cp)
+    return np.array(out, np.float64)
+
+
+@pytest.mark.skipif(not pyrefgpu.cages_available(), reason="reference cage cubin not built")
+@pytest.mark.parametrize("name", ["C3", "C5"])
+def test_dropin_cages_match_reference_gpu(bbpp_lib, name):
+    """cuda_build_cages of the drop-in against the reference's own cage builder
+    (its kernels of src/particle_kernel.cu under a restated one-rank
+    cuda_build_cages, compiled without FMA contraction as the host pin is) on
+    the same GPU, at the stated geometries: C3 (256^3, 1000 spheres of radius 6
+    cells) and C5 (512^3, 4000 spheres of radius 5 cells), with the periodic
+    copies the host program adds.  Phase, phase_shell and the three face-flag
+    arrays must agree element for element; the two builders' times are
+    printed."""
+    import time
+    from test_dropin import Host, make_dom
+    c = problems.CONFIGS[name]
+    g = problems.make_grid(c["n"], c["bc"])
+    cents, radii = problems.place_spheres(g, c["nsph"], c["rad"], c["seed"])
+    box = (g.nx * g.dx, g.ny * g.dy, g.nz * g.dz)
+    bc = tuple(int(v) for v in g.bc)
+    parts = with_periodic_copies(cents, radii, box, bc)
+    ref = pyrefgpu.RefCages(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, bc)
+    ref.build(parts)  # warm-up
+    *want, ms_ref = ref.build(parts)
+    raw = ref.parts_bytes(parts)
+    ref.close()
+    assert raw.shape[1] == 3128  # BB_PART_STRUCT_BYTES
+    H = Host()
+    H.dom = make_dom(g.nx, g.ny, g.nz, (g.dx, g.dy, g.dz))
+    H.g("dom", ctypes.c_void_p).value = ctypes.addressof(H.dom)
+    bcs = (ctypes.c_int * 6).in_dll(H.stub, "bc")
+    for i, b in enumerate(bc):
+        bcs[i] = b
+    H.g("rank", ctypes.c_int).value = 0
+    H.g("nprocs", ctypes.c_int).value = 1
+    H.g("NPARTS", ctypes.c_int).value = 1
+    H.g("nparts", ctypes.c_int).value = len(parts)
+    H.g("_parts", ctypes.c_void_p).value = H.dev(raw)
+    for nm, a in zip(("_phase", "_phase_shell", "_flag_u", "_flag_v", "_flag_w"), want):
+        H.g(nm, ctypes.c_void_p).value = H.dev(np.full(a.shape, 7, np.int32))
+    H.lib.cuda_build_cages()  # warm-up
+    bbpp.sync()
+    best = None
+    for _ in range(3):
+        t0 = time.perf_counter()
+        H.lib.cuda_build_cages()
+        bbpp.sync()
+        t = (time.perf_counter() - t0) * 1e3
+        best = t if best is None else min(best, t)
+    print("%s: %d particles; reference cage builder %.2f ms, drop-in %.3f ms (%.0fx)" % (
+        name, len(parts), ms_ref, best, ms_ref / best))
+    for nm, a in zip(("_phase", "_phase_shell", "_flag_u", "_flag_v", "_flag_w"), want):
+        out = np.empty(a.shape, np.int32)
+        bbpp.lib().bbpp_d2h(out.ctypes.data, H.g(nm, ctypes.c_void_p).value, out.nbytes)
+        assert np.array_equal(out, a), nm
+    assert (want[0] > -1).sum() > 0 and (want[1] == 0).sum() > 0
