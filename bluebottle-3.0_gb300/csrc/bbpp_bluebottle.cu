@@ -432,11 +432,11 @@ __global__ void k_add_const(Shape S, const double *__restrict__ neg_mean, double
 }
 
 // -------------------------------------------------------------- cages --
-// cuda_build_cages (src/cuda_particle.cu:1516-1646) in four launches instead of
+// cuda_build_cages (src/cuda_particle.cu:1516-1646) in six launches instead of
 // 2 x nparts serial launches with a host copy each: reset of phase and
 // phase_shell; one block per particle marking the cells of its cage inside it;
 // one block per particle clearing phase_shell on its boundary cells; one pass
-// over the three face arrays writing every flag.  The geometry is the
+// over each face array writing every flag.  The geometry is the
 // reference kernels' (cage_setup, build_phase, build_phase_shell,
 // src/particle_kernel.cu:134-426) in their evaluation order with no
 // contraction, so the cells marked are the same.  build_phase runs the
@@ -540,59 +540,83 @@ __global__ void __launch_bounds__(256) k_cage(CageGeom G, const unsigned char *_
   }
 }
 
-// Every face flag of the three face arrays (cage_flag_*, flag_external_*,
-// src/particle_kernel.cu:428-576): on the interior face planes -1 across a
-// phase change or between two shell cells, else 1; the ghost face planes 1;
-// both wall planes of a non-periodic direction 0.  Threads run each array in
-// its own memory order (flag_u [i][k][j], flag_v [j][i][k], flag_w [k][j][i]).
-__global__ void k_cage_flags(CageGeom G, int parts, const int *__restrict__ phase, const int *__restrict__ shell,
-                             int *__restrict__ fu, int *__restrict__ fv, int *__restrict__ fw) {
-  const int cx = G.cx, cy = G.cy, cz = G.cz;
-  const long long nu = (long long)(G.nx + 3) * cz * cy, nv = (long long)(G.ny + 3) * cx * cz,
-                  nw = (long long)(G.nz + 3) * cy * cx;
-  const long long total = nu + nv + nw;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    int a, b, plane, axis;  // (a, b) the in-plane indices in memory order, plane the face index along axis
-    long long c;
-    if (t < nu) {
-      c = t;
-      axis = 0;
-      a = (int)(c % cy);  // j
-      b = (int)((c / cy) % cz);  // k
-      plane = (int)(c / ((long long)cy * cz));  // i
-    } else if (t < nu + nv) {
-      c = t - nu;
-      axis = 1;
-      a = (int)(c % cz);  // k
-      b = (int)((c / cz) % cx);  // i
-      plane = (int)(c / ((long long)cz * cx));  // j
-    } else {
-      c = t - nu - nv;
-      axis = 2;
-      a = (int)(c % cx);  // i
-      b = (int)((c / cx) % cy);  // j
-      plane = (int)(c / ((long long)cx * cy));  // k
-    }
-    const int n = axis == 0 ? G.nx : (axis == 1 ? G.ny : G.nz);
+// The face flags (cage_flag_*, flag_external_*, src/particle_kernel.cu:428-576):
+// on the interior face planes -1 across a phase change or between two shell
+// cells, else 1; the ghost face planes 1; both wall planes of a non-periodic
+// direction 0.  The cell arrays run x fastest, flag_u [i][k][j] (y fastest)
+// and flag_v [j][i][k] (z fastest): their kernels read cells along x and go
+// through a 32 x 32 shared tile to write the flags along their own fastest
+// axis, so both sides are coalesced; flag_w [k][j][i] runs like the cells.
+__device__ __forceinline__ int face_flag(int parts, const int *__restrict__ phase, const int *__restrict__ shell,
+                                         long long lo, long long hi) {
+  if (!parts) return 1;
+  const bool flip = ((phase[lo] < 0) != (phase[hi] < 0)) || (shell[hi] < 1 && shell[lo] < 1);
+  return flip ? -1 : 1;
+}
+
+// flag_u: faces (i, j, k), i = 0 .. nx + 2; tile (i, j) of one k; block 32 x 8
+__global__ void __launch_bounds__(256) k_cage_flag_x(CageGeom G, int parts, const int *__restrict__ phase,
+                                                     const int *__restrict__ shell, int *__restrict__ fu) {
+  __shared__ int tile[32][33];
+  const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32, k = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool walls = G.wall[0] && G.wall[1];
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, j = j0 + r;
     int f = 1;
-    if (parts && plane >= 1 && plane <= n + 1) {
-      long long hi, lo;  // the cells on the two sides of the face
-      if (axis == 0) {
-        hi = plane + (long long)cx * (a + (long long)cy * b);
-        lo = hi - 1;
-      } else if (axis == 1) {
-        hi = b + (long long)cx * (plane + (long long)cy * a);
-        lo = hi - cx;
-      } else {
-        hi = a + (long long)cx * (b + (long long)cy * plane);
-        lo = hi - (long long)cx * cy;
+    if (i <= G.nx + 2 && j < G.cy) {
+      if (i >= 1 && i <= G.nx + 1) {
+        const long long hi = i + (long long)G.cx * (j + (long long)G.cy * k);
+        f = face_flag(parts, phase, shell, hi - 1, hi);
       }
-      const bool flip = ((phase[lo] < 0) != (phase[hi] < 0)) || (shell[hi] < 1 && shell[lo] < 1);
-      f = flip ? -1 : 1;
+      if (walls && (i == 1 || i == G.nx + 1)) f = 0;
     }
-    if (G.wall[2 * axis] && G.wall[2 * axis + 1] && (plane == 1 || plane == n + 1)) f = 0;
-    (axis == 0 ? fu : (axis == 1 ? fv : fw))[c] = f;
+    tile[r][tx] = f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, j = j0 + tx;
+    if (i <= G.nx + 2 && j < G.cy) fu[j + (long long)G.cy * (k + (long long)G.cz * i)] = tile[tx][r];
+  }
+}
+
+// flag_v: faces (i, j, k), j = 0 .. ny + 2; tile (i, k) of one j
+__global__ void __launch_bounds__(256) k_cage_flag_y(CageGeom G, int parts, const int *__restrict__ phase,
+                                                     const int *__restrict__ shell, int *__restrict__ fv) {
+  __shared__ int tile[32][33];
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32, j = blockIdx.z;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool walls = G.wall[2] && G.wall[3];
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, k = k0 + r;
+    int f = 1;
+    if (i < G.cx && k < G.cz) {
+      if (j >= 1 && j <= G.ny + 1) {
+        const long long hi = i + (long long)G.cx * (j + (long long)G.cy * k);
+        f = face_flag(parts, phase, shell, hi - G.cx, hi);
+      }
+      if (walls && (j == 1 || j == G.ny + 1)) f = 0;
+    }
+    tile[r][tx] = f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, k = k0 + tx;
+    if (i < G.cx && k < G.cz) fv[k + (long long)G.cz * (i + (long long)G.cx * j)] = tile[tx][r];
+  }
+}
+
+// flag_w: faces (i, j, k), k = 0 .. nz + 2 (blockIdx.y), in the cells' own order
+__global__ void k_cage_flag_z(CageGeom G, int parts, const int *__restrict__ phase, const int *__restrict__ shell,
+                              int *__restrict__ fw) {
+  const int plane = G.cx * G.cy, k = blockIdx.y;
+  const bool wall = G.wall[4] && G.wall[5] && (k == 1 || k == G.nz + 1);
+  const bool inner = k >= 1 && k <= G.nz + 1;
+  const long long base = (long long)plane * k;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < plane; c += gridDim.x * blockDim.x) {
+    int f = 1;
+    if (inner) f = face_flag(parts, phase, shell, base + c - plane, base + c);
+    fw[base + c] = wall ? 0 : f;
   }
 }
 
@@ -706,9 +730,13 @@ extern "C" void cuda_build_cages(void) {
       k_cage<1><<<nparts, 256>>>(G, reinterpret_cast<const unsigned char *>(_parts), _phase, _phase_shell);
     }
   }
-  const long long nf = (long long)(G.nx + 3) * G.cz * G.cy + (long long)(G.ny + 3) * G.cx * G.cz +
-                       (long long)(G.nz + 3) * G.cy * G.cx;
-  k_cage_flags<<<grid_blocks(nf), 256>>>(G, parts ? 1 : 0, _phase, _phase_shell, _flag_u, _flag_v, _flag_w);
+  const int pp = parts ? 1 : 0;
+  k_cage_flag_x<<<dim3((G.nx + 3 + 31) / 32, (G.cy + 31) / 32, G.cz), dim3(32, 8)>>>(G, pp, _phase, _phase_shell,
+                                                                                     _flag_u);
+  k_cage_flag_y<<<dim3((G.cx + 31) / 32, (G.cz + 31) / 32, G.ny + 3), dim3(32, 8)>>>(G, pp, _phase, _phase_shell,
+                                                                                     _flag_v);
+  k_cage_flag_z<<<dim3(std::min((G.cx * G.cy + 255) / 256, 128), G.nz + 3), 256>>>(G, pp, _phase, _phase_shell,
+                                                                                  _flag_w);
   check(cudaGetLastError(), "cage kernels");
 }
 

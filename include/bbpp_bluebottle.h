@@ -113,7 +113,7 @@ void cuda_update_p(void);
  * the face flags -1 across a phase change or between two shell cells; 0 on
  * both wall faces of a non-periodic direction.  Reads _parts[0 .. nparts-1]
  * (the host program's particles, periodic copies included, as the reference's
- * kernels do).  Four launches on the default stream, whatever nparts. */
+ * kernels do).  Six launches on the default stream, whatever nparts. */
 void cuda_build_cages(void);
 
 /* Free the library's private device workspace (no counterpart in the
