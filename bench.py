@@ -31,15 +31,16 @@ WORKLOAD = ("C3: 256^3 cells, periodic x/y + Neumann z, 1000 spheres r=6 cells, 
 # DRAM bytes (read + write) per launch of the dominant kernels on this workload,
 # from one ncu capture each (--set full, two launches of a 256^3 solve; the
 # summaries sit with the other profiles): kernel kind -> bytes
-NCU_TRAFFIC = {"search_spmv_f32": 226.697984e6 + 150.230784e6, "search_spmv": 433.925632e6 + 353.379328e6,
+NCU_TRAFFIC = {"search_spmv_f32": 226.697984e6 + 150.230784e6, "search_spmv": 432.974336e6 + 360.291072e6,
                "update_f32": 134.251008e6 + 20.922112e6, "update": 268.485376e6 + 92.526592e6,
                "fused_f32": 307.027712e6 + 216.193536e6}
 
 
 # FP64-pipe thread instructions per cell per launch of the plain FP64 kernels on
-# this workload, from one ncu capture of sm__thread_inst_executed_pipe_fp64_pred_on
-# (the summary sits with the other profiles): kernel kind -> instructions per cell
-NCU_FP64_INST = {"search_spmv": 155.67072e6 / 16777216, "update": 38.618304e6 / 16777216}
+# this workload (interior neighbour sums on the integer pipe), from one ncu
+# capture of sm__thread_inst_executed_pipe_fp64_pred_on (the summary sits with
+# the other profiles): kernel kind -> instructions per cell
+NCU_FP64_INST = {"search_spmv": 72.429664e6 / 16777216, "update": 38.618304e6 / 16777216}
 
 
 def peaks():

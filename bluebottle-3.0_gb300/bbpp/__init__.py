@@ -131,6 +131,8 @@ def lib():
         "bbpp_set_profiling": (I, [P, I]),
         "bbpp_set_fused": (I, [P, I]),
         "bbpp_set_ff_resid": (I, [P, I]),
+        "bbpp_set_xsum": (I, [P, I]),
+        "bbpp_neighbour_sums": (I, [P, P, ctypes.c_longlong]),
         "bbpp_rng_uniform": (None, [ctypes.c_ulonglong, ctypes.c_longlong, D, D, P]),
         "bbpp_rng_gauss": (None, [ctypes.c_ulonglong, ctypes.c_longlong, P]),
         "bbpp_version": (ctypes.c_char_p, []),
@@ -319,6 +321,12 @@ class Solver:
         """Reliable-update residuals in float-float (True) or FP64 arithmetic."""
         _check(lib().bbpp_set_ff_resid(self.handle, 1 if on else 0))
 
+    def set_xsum(self, on):
+        """FP64 stencils on an isotropic grid (the plain iteration's search
+        kernel, the FP64 residuals): interior neighbour sums as exact
+        fixed-point sums on the integer pipe (True) or FP64 adds."""
+        _check(lib().bbpp_set_xsum(self.handle, 1 if on else 0))
+
     def kernel_stats(self):
         arr = (KStat * 32)()
         n = ctypes.c_int()
@@ -373,6 +381,16 @@ def stream_mix_rate(cells):
     v = ctypes.c_double()
     _check(lib().bbpp_stream_mix_rate(int(cells), ctypes.byref(v)))
     return v.value
+
+
+def neighbour_sums(v):
+    """The FP64 search kernel's neighbour sum of each row of an (n, 6) float64
+    array, computed on the GPU (bbpp_neighbour_sums)."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    assert v.ndim == 2 and v.shape[1] == 6
+    out = np.empty(v.shape[0], np.float64)
+    _check(lib().bbpp_neighbour_sums(v.ctypes.data, out.ctypes.data, v.shape[0]))
+    return out
 
 
 def fp64_fma_rate():

@@ -44,6 +44,7 @@ struct GeoL {
   int nx, ny, nz;
   int px, py, pz;
   int iso;             // ax == ay == az
+  int xsum;            // FP64 stencils, iso: interior neighbour sums on the integer pipe (xsum6)
   long long n;
   double S;            // scale of L = S (-A)
   double ax, ay, az;   // S/dx^2, S/dy^2, S/dz^2
@@ -95,6 +96,90 @@ __device__ __forceinline__ T apply_L(const GeoL &G, const T *s_dL, int cls, T pc
     if (cls == 0) return pc - s;
     return fma(s_dL[cls], pc, -s);
   }
+}
+
+// ---------------------------------------------- exact neighbour sums ---
+// The six-neighbour sum of the isotropic stencil in FP64 as one fixed-point
+// sum on the integer pipe, rounded once to nearest even.  GB300 issues FP64 at
+// 1/64 of its FP32 rate, and the five FP64 adds kept the FP64 search kernel on
+// that pipe; the ~150 integer operations below run beside the remaining FP64
+// work (at 256^3 the kernel went from 370 to 311 us per launch).
+//
+// Each 53-bit significand is aligned to the largest exponent of the six, the
+// largest value's leading bit at bit 59 of a signed 64-bit accumulator; bits
+// shifted below bit 0 are dropped, under one unit (2^-59 of the largest
+// value's leading bit) per value.  Six aligned magnitudes stay below 6 * 2^60
+// < 2^63, so the accumulator cannot overflow.  The result lies within 1/2 ulp
+// of the exact sum plus six units (ulp(max)/128), against five roundings of up
+// to 1/2 ulp each for the FP64 adds.  Returns false, with `out` unset, when
+// the largest biased exponent lies outside [128, 2040] (all six zero or tiny,
+// or an Inf or NaN).
+__device__ __forceinline__ bool xsum6(const double (&v)[6], double &out) {
+  // biased exponent << 20 of the largest magnitude
+  unsigned int E = 0;
+#pragma unroll
+  for (int i = 0; i < 6; i++) E = max(E, (unsigned int)__double2hiint(v[i]) & 0x7ff00000u);
+  if (E < (128u << 20) || E > (2040u << 20)) return false;
+  // A value of exponent field e shifts right by E - e + 4.  Zero and
+  // subnormal values (e = 0) have no leading bit and lie below 2^-1022, under
+  // 2^-68 of one unit (E >= 128), so any shift of 63 or more drops them.
+  const unsigned int Ep = E + (4u << 20);
+  long long acc = 0;
+#pragma unroll
+  for (int i = 0; i < 6; i++) {
+    const unsigned int hi = (unsigned int)__double2hiint(v[i]), lo = (unsigned int)__double2loint(v[i]);
+    const unsigned int raw = hi & 0x7ff00000u;
+    // significand left-aligned in 64 bits: fraction at bits 62..11, the
+    // leading bit (set iff the exponent field is non-zero) at bit 63
+    unsigned int whi = __funnelshift_l(lo, hi, 11);
+    whi = (whi & 0x7fffffffu) | ((raw + 0x7fffffffu) & 0x80000000u);
+    const unsigned int sh = min((Ep - raw) >> 20, 63u);
+    const long long w = (long long)((((unsigned long long)whi << 32) | (unsigned long long)(lo << 11)) >> sh);
+    const long long sg = (long long)((int)hi >> 31);
+    acc += (w ^ sg) - sg;
+  }
+  // value = acc * 2^(E - 1082), rounded once to nearest even in integer
+  // arithmetic (a conversion instruction would run on the FP64 pipe)
+  const long long sg = acc >> 63;
+  unsigned long long m = (unsigned long long)((acc ^ sg) - sg);
+  if (m == 0ull) {
+    out = 0.0;
+    return true;
+  }
+  const int lz = __clzll((long long)m);  // >= 1: |acc| < 2^63
+  m <<= lz;
+  const unsigned long long mant = m >> 11;  // 53 bits, leading bit at 52
+  const unsigned int rest = (unsigned int)m & 0x7ffu;
+  const unsigned long long up = (rest > 0x400u || (rest == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+  // biased exponent E + 4 - lz, of which the leading bit of mant adds one; a
+  // carry out of the rounding adds another
+  const unsigned long long bits = ((unsigned long long)((E >> 20) + 3u - (unsigned int)lz) << 52) + mant + up;
+  out = __longlong_as_double((long long)(bits | ((unsigned long long)sg & 0x8000000000000000ull)));
+  return true;
+}
+
+// The isotropic neighbour sum of FP64 p: xsum6 where it applies, FP64 adds in
+// the stencil's order otherwise.  A solid cell (`skip`) discards its result, so
+// it never takes the FP64 branch.
+__device__ __forceinline__ double nb_sum6(double pe, double pw, double pn, double ps, double pt, double pb,
+                                          bool skip) {
+  const double v[6] = {pe, pw, pn, ps, pt, pb};
+  double s;
+  if (!xsum6(v, s)) s = skip ? 0.0 : ((pe + pw) + (pn + ps)) + (pt + pb);
+  return s;
+}
+
+// L p at an interior cell (class 0): apply_L, or for FP64 on an isotropic grid
+// with G.xsum set, the centre minus ax times the exact neighbour sum.
+template <typename T, bool ISO>
+__device__ __forceinline__ T apply_L0(const GeoL &G, T pc, T pe, T pw, T pn, T ps, T pt, T pb, bool skip) {
+  return apply_L<T, ISO>(G, nullptr, 0, pc, pe, pw, pn, ps, pt, pb);
+}
+template <>
+__device__ __forceinline__ double apply_L0<double, true>(const GeoL &G, double pc, double pe, double pw, double pn,
+                                                         double ps, double pt, double pb, bool skip) {
+  if (!G.xsum) return apply_L<double, true>(G, nullptr, 0, pc, pe, pw, pn, ps, pt, pb);
+  return fma(-G.ax, nb_sum6(pe, pw, pn, ps, pt, pb, skip), pc);
 }
 
 // ------------------------------------------------------------ K1, pairs ---
@@ -347,8 +432,8 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
       const T w = sp[sc][ly][col - 1], e = sp[sc][ly][col + 2];
       T a0, a1;
       if (interior) {
-        a0 = apply_L<T, ISO>(G, s_dL, 0, c.x, c.y, w, n.x, s.x, t.x, b.x);
-        a1 = apply_L<T, ISO>(G, s_dL, 0, c.y, e, c.x, n.y, s.y, t.y, b.y);
+        a0 = apply_L0<T, ISO>(G, c.x, c.y, w, n.x, s.x, t.x, b.x, MASK && mk[h][0]);
+        a1 = apply_L0<T, ISO>(G, c.y, e, c.x, n.y, s.y, t.y, b.y, MASK && mk[h][1]);
       } else {
         const int cy = (h ? cy1 : cy0) + wz;
         a0 = apply_L<T, ISO>(G, s_dL, wxp0 + cy, c.x, c.y, w, n.x, s.x, t.x, b.x);
@@ -676,7 +761,8 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       TXT pn = sp[sc][ly + 1][lx], ps = sp[sc][ly - 1][lx];
       TXT pt = sp[st_][ly][lx], pb = sp[sb][ly][lx];
       const int cls = INTERIOR ? 0 : wall_count(gx, nx, G.px) + 3 * wall_count(gy, ny, G.py) + 9 * wall_count(z, nz, G.pz);
-      const TXT a = apply_L<TXT, ISO>(G, s_dL, cls, pc, pe, pw, pn, ps, pt, pb);
+      const TXT a = INTERIOR ? apply_L0<TXT, ISO>(G, pc, pe, pw, pn, ps, pt, pb, false)
+                             : apply_L<TXT, ISO>(G, s_dL, cls, pc, pe, pw, pn, ps, pt, pb);
       const TXT rv = fma((TXT)bscale, bv, -a);
       const TR ro = (TR)rv;
       rout[c] = ro;

@@ -285,6 +285,11 @@ extern "C" int bbpp_create(const bbpp_grid *g, bbpp_ctx **out) {
     // arithmetic on the FP32 pipe (~48 bits; measured 0.2 ms per C3 solve)
     const char *ff = getenv("BBPP_FF_RESID");
     ctx->ff_resid = ff && ff[0] == '1';
+    // FP64 stencils on an isotropic grid (search kernel, residuals): interior
+    // neighbour sums as exact fixed-point sums on the integer pipe
+    // (BBPP_XSUM=0: FP64 adds)
+    const char *xs = getenv("BBPP_XSUM");
+    ctx->GL.xsum = !(xs && xs[0] == '0');
   }
   const size_t n = (size_t)ctx->G.n;
   const size_t nparts = std::max<size_t>(
@@ -1314,6 +1319,33 @@ extern "C" int bbpp_fp64_fma_rate(double *fma_per_s) {
   return 0;
 }
 
+// nb_sum6 over n six-tuples (the FP64 search kernel's interior neighbour sum)
+__global__ void k_nb_sum6(const double *__restrict__ in, double *__restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double *v = in + 6 * i;
+    out[i] = nb_sum6(v[0], v[1], v[2], v[3], v[4], v[5], false);
+  }
+}
+
+extern "C" int bbpp_neighbour_sums(const double *in, double *out, long long n) {
+  bbpp_ctx *ctx = nullptr;
+  if (n < 0 || (n > 0 && (!in || !out)) || n > (1ll << 26)) return BBPP_BAD_ARG;
+  if (n == 0) return 0;
+  double *d_in = nullptr, *d_out = nullptr;
+  cudaError_t e = cudaMalloc(&d_in, sizeof(double) * 6 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMemcpy(d_in, in, sizeof(double) * 6 * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_nb_sum6<<<(unsigned)std::min<long long>((n + 255) / 256, 4096), 256>>>(d_in, d_out, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d_out, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(d_in);
+  cudaFree(d_out);
+  CK(e);
+  return 0;
+}
+
 // The bandwidth a plain streaming kernel reaches with the fused FP32
 // iteration's per-cell traffic: four FP32 reads, one mask byte, four FP32
 // writes (33 B/cell), elementwise, no stencil.  It separates what the traffic
@@ -1439,6 +1471,13 @@ extern "C" int bbpp_set_ff_resid(bbpp_ctx *ctx, int on) {
   if (!ctx || (on != 0 && on != 1)) return BBPP_BAD_ARG;
   ctx->ff_resid = on == 1;
   drop_graphs(ctx);  // the replacement kernels are captured in the iteration graphs
+  return 0;
+}
+
+extern "C" int bbpp_set_xsum(bbpp_ctx *ctx, int on) {
+  if (!ctx || (on != 0 && on != 1)) return BBPP_BAD_ARG;
+  ctx->GL.xsum = on;
+  drop_graphs(ctx);  // the geometry is a parameter of the captured kernels
   return 0;
 }
 

@@ -201,6 +201,10 @@ int bbpp_fp64_fma_rate(double *fma_per_s);
  * launches, the best kept).  Allocates its buffers (about 33 B per cell) for
  * the measurement.  No counterpart in the reference. */
 int bbpp_stream_mix_rate(long long cells, double *bytes_per_s);
+/* out[i] = the FP64 search kernel's neighbour sum of in[6i .. 6i+5] (host
+ * buffers, n <= 2^26): the fixed-point sum, or FP64 adds where all six are
+ * zero or tiny or one is not finite.  For tests of that arithmetic. */
+int bbpp_neighbour_sums(const double *in, double *out, long long n);
 /* Page-locked host memory (for end-to-end timing from pinned buffers). */
 int bbpp_host_alloc(size_t bytes, void **ptr);
 int bbpp_host_free(void *ptr);
@@ -226,6 +230,13 @@ int bbpp_set_fused(bbpp_ctx *ctx, int on);
  * residual): 0 = FP64 arithmetic (the default), 1 = float-float arithmetic on
  * the FP32 pipe (about 48 bits). */
 int bbpp_set_ff_resid(bbpp_ctx *ctx, int on);
+/* FP64 stencils on a grid with dx = dy = dz (the plain iteration's search
+ * kernel and the FP64 residuals of both methods): 1 = each interior cell's
+ * six-neighbour sum as an exact fixed-point sum on the integer pipe, rounded
+ * once (the default; within 1/2 ulp plus ulp(max)/128 of the exact sum),
+ * 0 = five FP64 adds.  No counterpart in the reference, whose stencil adds in
+ * FP64 (src/solver_kernel.cu:691-707). */
+int bbpp_set_xsum(bbpp_ctx *ctx, int on);
 
 /* ---- learned initial guess (no counterpart in the reference) ----
  * A 3-level 3D conv encoder-decoder (channels 16/32/64, 3x3x3 kernels, BF16
