@@ -684,23 +684,24 @@ __device__ __forceinline__ double widen(float f) {
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e32 - 127u + 1023u) << 52) | frac));
 }
 
-// The warm start's residual r = rhs - (-A) p_prev, restricted by 2 in the same
-// pass (cell-centred: the means of the 2x2x2 children), with p_prev's means
-// and the coarse solid cells (at least 4 solid children).  The residual is
+// The warm start's residual r = rhs - (-A) p_prev, restricted by F (2 or 4) in
+// the same pass (cell-centred: the means of the FxFxF children), with p_prev's
+// means and the coarse solid cells (at least half the children solid).  The residual is
 // formed as in the residual kernel (k_resid: neighbours of or across solid
 // cells count 0, walls through the class diagonal) but in FP32 arithmetic, on
 // inputs narrowed by truncation (narrow_rz): it only feeds the BF16 network.
 // prev == NULL: r = rhs, p_prev = 0.
-__global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, const double *__restrict__ rhs,
-                                                         const double *__restrict__ prev,
-                                                         const uint8_t *__restrict__ mask, double *__restrict__ rc,
-                                                         double *__restrict__ pc, uint8_t *__restrict__ mc) {
+template <int F>
+__global__ void __launch_bounds__(256) k_resid_restrict(const bbpp::Geo G, const double *__restrict__ rhs,
+                                                        const double *__restrict__ prev,
+                                                        const uint8_t *__restrict__ mask, double *__restrict__ rc,
+                                                        double *__restrict__ pc, uint8_t *__restrict__ mc) {
   __shared__ float s_tab[81];
   for (int e = threadIdx.x; e < 81; e += blockDim.x) s_tab[e] = (float)G.tab[e];
   __syncthreads();
   const int nx = G.nx, ny = G.ny, nz = G.nz;
-  const unsigned int cxn = (unsigned)nx >> 1, cyn = (unsigned)ny >> 1;
-  const unsigned int nc = cxn * cyn * ((unsigned)nz >> 1);
+  const unsigned int cxn = (unsigned)nx / F, cyn = (unsigned)ny / F;
+  const unsigned int nc = cxn * cyn * ((unsigned)nz / F);
   const float fx = (float)G.cx, fy = (float)G.cy, fz = (float)G.cz;
   // p_prev at a neighbour (0 outside a wall); solid: the neighbour is solid
   auto nb = [&](int xx, int yy, int zz, bool &solid) -> float {
@@ -716,9 +717,9 @@ __global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, cons
     const unsigned int i = e % cxn, t = e / cxn, j = t % cyn, k = t / cyn;
     float sr = 0.f, sp = 0.f;
     int sm = 0;
-#pragma unroll
-    for (int ch = 0; ch < 8; ch++) {
-      const int x = 2 * (int)i + (ch & 1), y = 2 * (int)j + ((ch >> 1) & 1), z = 2 * (int)k + (ch >> 2);
+#pragma unroll 8
+    for (int ch = 0; ch < F * F * F; ch++) {
+      const int x = F * (int)i + ch % F, y = F * (int)j + (ch / F) % F, z = F * (int)k + ch / (F * F);
       const unsigned int c = (unsigned)x + (unsigned)nx * ((unsigned)y + (unsigned)ny * (unsigned)z);
       const bool ms = mask && mask[c] != 0;
       float r = narrow_rz(rhs[c]);
@@ -747,9 +748,10 @@ __global__ void __launch_bounds__(256) k_resid_restrict2(const bbpp::Geo G, cons
       sr += r;
       sm += ms ? 1 : 0;
     }
-    rc[e] = 0.125 * (double)sr;
-    pc[e] = 0.125 * (double)sp;
-    mc[e] = sm >= 4 ? 1 : 0;
+    constexpr double inv = 1.0 / (F * F * F);
+    rc[e] = inv * (double)sr;
+    pc[e] = inv * (double)sp;
+    mc[e] = sm >= F * F * F / 2 ? 1 : 0;
   }
 }
 
@@ -761,19 +763,20 @@ __global__ void k_corr2(float *__restrict__ corr, const double *__restrict__ p0c
     corr[e] = mc[e] ? 0.f : (float)(p0c[e] - pc[e]);
 }
 
-// one axis of the cell-centred trilinear prolongation by 2: fine cell a lies
-// at coarse coordinate a/2 - 1/4, between coarse cells lo and hi, hi weighted w
+// one axis of the cell-centred trilinear prolongation by F: fine cell a = F m + q
+// lies at coarse coordinate m + (2q + 1 - F) / (2F), between coarse cells lo
+// and hi, hi weighted w (F = 2: a/2 - 1/4)
+template <int F>
 __device__ __forceinline__ void prolong_axis(int a, int n, int periodic, int &lo, int &hi, float &w) {
-  const int m = a >> 1;
-  if (a & 1) {
-    lo = m;
-    hi = m + 1;
-    w = 0.25f;
-  } else {
+  const int m = a / F, num = 2 * (a - m * F) + 1 - F;
+  if (num < 0) {
     lo = m - 1;
-    hi = m;
-    w = 0.75f;
+    w = (float)(2 * F + num) / (float)(2 * F);
+  } else {
+    lo = m;
+    w = (float)num / (float)(2 * F);
   }
+  hi = lo + 1;
   if (periodic) {
     lo = lo < 0 ? lo + n : lo;
     hi = hi >= n ? hi - n : hi;
@@ -786,10 +789,11 @@ __device__ __forceinline__ void prolong_axis(int a, int n, int periodic, int &lo
 // x = p_prev + the trilinear interpolation of the coarse correction (FP32,
 // widened exactly before the FP64 add); fine solid cells 0, as the guess on
 // the grid itself
-__global__ void __launch_bounds__(256) k_prolong2(const float *__restrict__ corr, const double *__restrict__ prev,
-                                                  const uint8_t *__restrict__ mask, int nx, int ny, int nz, int px,
-                                                  int py, int pz, double *__restrict__ x) {
-  const int cxn = nx >> 1, cyn = ny >> 1, czn = nz >> 1;
+template <int F>
+__global__ void __launch_bounds__(256) k_prolong(const float *__restrict__ corr, const double *__restrict__ prev,
+                                                 const uint8_t *__restrict__ mask, int nx, int ny, int nz, int px,
+                                                 int py, int pz, double *__restrict__ x) {
+  const int cxn = nx / F, cyn = ny / F, czn = nz / F;
   const unsigned int n = (unsigned)nx * (unsigned)ny * (unsigned)nz;
   for (unsigned int f = blockIdx.x * 256u + threadIdx.x; f < n; f += gridDim.x * 256u) {
     if (mask && mask[f]) {
@@ -801,9 +805,9 @@ __global__ void __launch_bounds__(256) k_prolong2(const float *__restrict__ corr
     const int k = (int)(t / (unsigned)ny), j = (int)(t - (unsigned)k * (unsigned)ny);
     int xl, xh, yl, yh, zl, zh;
     float wx, wy, wz;
-    prolong_axis(i, cxn, px, xl, xh, wx);
-    prolong_axis(j, cyn, py, yl, yh, wy);
-    prolong_axis(k, czn, pz, zl, zh, wz);
+    prolong_axis<F>(i, cxn, px, xl, xh, wx);
+    prolong_axis<F>(j, cyn, py, yl, yh, wy);
+    prolong_axis<F>(k, czn, pz, zl, zh, wz);
     const unsigned int r00 = ((unsigned)zl * cyn + yl) * cxn, r01 = ((unsigned)zl * cyn + yh) * cxn;
     const unsigned int r10 = ((unsigned)zh * cyn + yl) * cxn, r11 = ((unsigned)zh * cyn + yh) * cxn;
     const float a00 = (1.f - wx) * corr[r00 + xl] + wx * corr[r00 + xh];
@@ -1425,25 +1429,27 @@ static void drop_guess_graphs(NetWork *w) {
   w->graphs.clear();
 }
 
-// The learned guess of a solve.  coarsen 2: the network runs on the problem
-// restricted by 2 (k_restrict2) with h^2 scaled by 4, and its correction comes
-// back by trilinear interpolation (k_prolong2); at 256^3 this both costs 1/8
-// of the inference and gives a better guess (the network sees twice as far in
-// fine cells).  coarsen 0 picks 2 when every extent is a multiple of 8 and at
-// least 128.
+// The learned guess of a solve.  coarsen F = 2 or 4: the network runs on the
+// problem restricted by F (k_resid_restrict) with h^2 scaled by F^2, and its
+// correction comes back by trilinear interpolation (k_prolong); at 256^3 and
+// F = 2 this both costs 1/8 of the inference and gives a better guess (the
+// network sees twice as far in fine cells).  F needs every extent a multiple
+// of 4F (the network pools twice).  coarsen 0 picks 2 when every extent is a
+// multiple of 8 and at least 128.
 int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double *rhs, const double *prev, double *x,
                    int coarsen, double *ms) {
   bbpp_net *n = (bbpp_net *)netp;
   if (!n) return BBPP_BAD_ARG;
   const int nx = ctx->G.nx, ny = ctx->G.ny, nz = ctx->G.nz;
-  const bool fits2 = nx % 8 == 0 && ny % 8 == 0 && nz % 8 == 0;
+  auto fits = [&](int F) { return nx % (4 * F) == 0 && ny % (4 * F) == 0 && nz % (4 * F) == 0; };
   int f = coarsen;
-  if (f == 0) f = (fits2 && std::min(nx, std::min(ny, nz)) >= 128) ? 2 : 1;
-  if (f == 2 && !fits2) return BBPP_BAD_ARG;
-  if (f == 2) {
+  if (f == 0) f = (fits(2) && std::min(nx, std::min(ny, nz)) >= 128) ? 2 : 1;
+  if (f != 1 && f != 2 && f != 4) return BBPP_BAD_ARG;
+  if (f > 1 && !fits(f)) return BBPP_BAD_ARG;
+  if (f > 1) {
     if (!ctx->net) ctx->net = new NetWork();
     NetWork *w = ctx->net;
-    const long long nc = (long long)(nx / 2) * (ny / 2) * (nz / 2);
+    const long long nc = (long long)(nx / f) * (ny / f) * (nz / f);
     if (w->ncap < nc) {
       cudaFree(w->rc);
       cudaFree(w->pc);
@@ -1480,19 +1486,27 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
       rc_ = bbpp_residual_async(ctx, mask, rhs, prev, ctx->Ap);
       r = ctx->Ap;
     }
-    if (f == 2) {
+    if (f > 1) {
       NetWork *w = ctx->net;
-      const long long nc = (long long)(nx / 2) * (ny / 2) * (nz / 2);
+      const long long nc = (long long)(nx / f) * (ny / f) * (nz / f);
       if (rc_ == 0) {
-        k_resid_restrict2<<<nblocks(nc), 256, 0, ctx->stream>>>(ctx->G, rhs, prev, mask, w->rc, w->pc, w->mc);
+        if (f == 2)
+          k_resid_restrict<2><<<nblocks(nc), 256, 0, ctx->stream>>>(ctx->G, rhs, prev, mask, w->rc, w->pc, w->mc);
+        else
+          k_resid_restrict<4><<<nblocks(nc), 256, 0, ctx->stream>>>(ctx->G, rhs, prev, mask, w->rc, w->pc, w->mc);
         if (cudaGetLastError() != cudaSuccess) rc_ = BBPP_CUDA_ERROR;
       }
       if (rc_ == 0)
-        rc_ = bbpp_net_infer(n, nx / 2, ny / 2, nz / 2, 4.0 * h2, w->rc, w->pc, mask ? w->mc : nullptr, w->p0c);
+        rc_ = bbpp_net_infer(n, nx / f, ny / f, nz / f, (double)(f * f) * h2, w->rc, w->pc, mask ? w->mc : nullptr,
+                             w->p0c);
       if (rc_ == 0) {
         k_corr2<<<nblocks(nc), 256, 0, ctx->stream>>>(w->corr, w->p0c, w->pc, w->mc, (unsigned)nc);
-        k_prolong2<<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->corr, prev, mask, nx, ny, nz, ctx->G.px, ctx->G.py,
-                                                                ctx->G.pz, x);
+        if (f == 2)
+          k_prolong<2><<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->corr, prev, mask, nx, ny, nz, ctx->G.px,
+                                                                   ctx->G.py, ctx->G.pz, x);
+        else
+          k_prolong<4><<<nblocks(ctx->G.n), 256, 0, ctx->stream>>>(w->corr, prev, mask, nx, ny, nz, ctx->G.px,
+                                                                   ctx->G.py, ctx->G.pz, x);
         if (cudaGetLastError() != cudaSuccess) rc_ = BBPP_CUDA_ERROR;
       }
       *count = (n->launches - l0) + 3;
@@ -1509,7 +1523,7 @@ int bbpp_net_guess(bbpp_ctx *ctx, void *netp, const uint8_t *mask, const double 
   NetWork *gw = ctx->net;
   // the network's workspace for this grid exists before the key is taken
   if (!(ge && ge[0] == '0')) {
-    const int wnx = f == 2 ? nx / 2 : nx, wny = f == 2 ? ny / 2 : ny, wnz = f == 2 ? nz / 2 : nz;
+    const int wnx = nx / f, wny = ny / f, wnz = nz / f;
     if (!(n->wx == wnx && n->wy == wny && n->wz == wnz && n->wb == 1)) rc = ensure_work(n, wnx, wny, wnz, 1, false);
   }
   const GuessKey key = {n->uid, n->gen, mask, rhs, prev, x, f, conv_tc_mode(), g_tc_max_ctas};

@@ -936,7 +936,7 @@ static int check_opts(const bbpp_opts *o) {
   if (!(o->ir_drop >= 0.0 && o->ir_drop < 1.0)) return BBPP_BAD_ARG;
   if (!(o->tol >= 0) || o->max_iter < 0 || o->replace_every < 1) return BBPP_BAD_ARG;
   if (o->guess == BBPP_GUESS_LEARNED && !o->net) return BBPP_BAD_ARG;
-  if (o->net_coarsen < 0 || o->net_coarsen > 2) return BBPP_BAD_ARG;
+  if (o->net_coarsen < 0 || o->net_coarsen > 4 || o->net_coarsen == 3) return BBPP_BAD_ARG;
   return 0;
 }
 

@@ -94,9 +94,9 @@ typedef struct bbpp_opts {
                          residual once ||r|| has dropped by this factor since the last replacement (and at
                          least every 8 checkpoints); 0 = at every checkpoint.  Default 1e-2. */
   int net_coarsen;    /* GUESS_LEARNED: the network runs on the grid coarsened by this factor, 1 (the
-                         grid itself) or 2 (the mean of 2x2x2 cells; the correction comes back by
-                         trilinear interpolation); 0 (default) = 2 when every extent is even and at
-                         least 128, else 1 */
+                         grid itself), 2 or 4 (the means of FxFxF cells, every extent a multiple of
+                         4F; the correction comes back by trilinear interpolation); 0 (default) = 2
+                         when every extent is a multiple of 8 and at least 128, else 1 */
 } bbpp_opts;
 
 typedef struct bbpp_report {

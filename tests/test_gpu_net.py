@@ -241,18 +241,18 @@ def test_net_checkpoint_roundtrip(bbpp_lib, tmp_path):
     assert np.array_equal(other.get_params(), p)
 
 
-def _restrict2(a):
+def _restrict(a, F):
     nz, ny, nx = a.shape
-    return a.reshape(nz // 2, 2, ny // 2, 2, nx // 2, 2).mean(axis=(1, 3, 5))
+    return a.reshape(nz // F, F, ny // F, F, nx // F, F).mean(axis=(1, 3, 5))
 
 
-def _prolong2(c, periodic):
-    """Cell-centred trilinear interpolation by 2 (weights 3/4, 1/4 per axis);
-    periodic axes wrap, the others repeat the edge cell.  Axes [z, y, x]."""
+def _prolong(c, periodic, F):
+    """Cell-centred trilinear interpolation by F (F = 2: weights 3/4, 1/4 per
+    axis); periodic axes wrap, the others repeat the edge cell.  Axes [z, y, x]."""
     out = c
     for ax in range(3):
         n = out.shape[ax]
-        fi = (np.arange(2 * n) + 0.5) / 2 - 0.5
+        fi = (np.arange(F * n) + 0.5) / F - 0.5
         lo = np.floor(fi).astype(int)
         w = fi - lo
         if periodic[ax]:
@@ -265,18 +265,21 @@ def _prolong2(c, periodic):
     return out
 
 
+@pytest.mark.parametrize("F", [2, 4])
 @pytest.mark.parametrize("bc", ["ppn", "nnn"])
-def test_coarse_guess_matches_restatement(bbpp_lib, bc):
-    """The learned guess on the grid restricted by 2: the solver's guess equals
-    p_prev + prolong2(net(restrict2(r, p_prev, mask)) - restrict2(p_prev)), with
-    the network run directly on numpy-restricted inputs, coarse solid cells
-    (>= 4 solid children) carrying no correction and fine solid cells 0."""
-    nx, ny, nz = 32, 16, 24
+def test_coarse_guess_matches_restatement(bbpp_lib, bc, F):
+    """The learned guess on the grid restricted by F: the solver's guess equals
+    p_prev + prolong_F(net(restrict_F(r, p_prev, mask)) - restrict_F(p_prev)),
+    with the network run directly on numpy-restricted inputs, coarse solid
+    cells (at least half the children solid) carrying no correction and fine
+    solid cells 0."""
+    nx, ny, nz = 32, 16, 48
     g = problems.make_grid(nx, bc, ny=ny, nz=nz)
     rng = np.random.default_rng(5)
     mask = np.zeros((nz, ny, nx), np.uint8)
     mask[6:11, 3:8, 10:17] = 1
     mask[15:17, 9:12, 2:4] = 1
+    mask[28:37, 4:12, 16:24] = 1
     rhs = rng.normal(size=(nz, ny, nx))
     rhs[mask == 1] = 0
     prev = rng.normal(size=(nz, ny, nx))
@@ -285,21 +288,22 @@ def test_coarse_guess_matches_restatement(bbpp_lib, bc):
     net = learned.Net(seed=4)
     dx = bbpp.DeviceArray((nz, ny, nx), np.float64)
     rep = s.solve(drhs, dx, dmask, tol=1e300, precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle,
-                  prev=dprev.ptr, net_coarsen=2)
+                  prev=dprev.ptr, net_coarsen=F)
     assert rep.iters == 0
     got = dx.download()
     # the same on the host: residual of the warm start (solver's kernel), restriction, network, prolongation
     dr = bbpp.DeviceArray((nz, ny, nx), np.float64)
     s.residual(drhs, dprev, dr, dmask)
     r = dr.download()
-    rc, pc = _restrict2(r), _restrict2(prev)
-    mc = (_restrict2(mask.astype(np.float64)) >= 0.5).astype(np.uint8)
+    rc, pc = _restrict(r, F), _restrict(prev, F)
+    mc = (_restrict(mask.astype(np.float64), F) >= 0.5).astype(np.uint8)
+    assert mc.any()
     d_rc, d_pc, d_mc = (bbpp.DeviceArray.from_host(a) for a in (rc, pc, mc))
     d_o = bbpp.DeviceArray(rc.shape, np.float64)
-    net.infer((nx // 2, ny // 2, nz // 2), 4 * g.dx * g.dy, d_rc, d_pc, d_mc, d_o)
+    net.infer((nx // F, ny // F, nz // F), F * F * g.dx * g.dy, d_rc, d_pc, d_mc, d_o)
     corr = np.where(mc == 1, 0.0, d_o.download() - pc)
     periodic = [bc[2] == "p", bc[1] == "p", bc[0] == "p"]
-    want = np.where(mask == 1, 0.0, prev + _prolong2(corr, periodic))
+    want = np.where(mask == 1, 0.0, prev + _prolong(corr, periodic, F))
     scale = np.abs(want - prev).max()
     assert scale > 0
     # the solver forms the residual inside its restriction in FP32 arithmetic,
@@ -307,6 +311,23 @@ def test_coarse_guess_matches_restatement(bbpp_lib, bc):
     assert np.abs(got - want).max() <= 1e-2 * scale
     assert np.abs(got - want).mean() <= 1e-3 * scale
     net.close()
+
+
+def test_coarsen_rejects_unfit_grids(bbpp_lib):
+    """Restriction by F needs every extent a multiple of 4F: 3 is no factor,
+    and 24 cells cannot be restricted by 4."""
+    g = problems.make_grid(24, "ppn")
+    s = bbpp.Solver(g)
+    net = learned.Net(seed=4)
+    drhs = bbpp.DeviceArray.from_host(np.zeros(g.shape))
+    dx = bbpp.DeviceArray(g.shape, np.float64)
+    for F in (3, 4):
+        with pytest.raises(bbpp.BbppError) as e:
+            s.solve(drhs, dx, None, tol=1e300, precision=bbpp.FP32_IR, guess=bbpp.GUESS_LEARNED, net=net.handle,
+                    net_coarsen=F)
+        assert e.value.status == bbpp.BAD_ARG
+    net.close()
+    s.close()
 
 
 def test_learned_guess_gain(bbpp_lib):
