@@ -116,6 +116,44 @@ inline void bbpp_launch(const bbpp_ctx *ctx, void (*kern)(KArgs...), dim3 grid, 
   cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
+// z chunking of a kernel whose CTAs each own one of `units` columns (tiles or
+// slabs) for one chunk of planes, `slots` CTAs resident at once: returns the
+// number of chunks and sets *kz (planes per chunk, at least min_kz where nz
+// allows).  One wave of slots / units chunks while that fills at least 90% of
+// the resident CTAs.  Otherwise (at 512^3, 256 tile columns against 456 slots
+// leave a single wave 56% full) the count that minimises waves x (kz + 2),
+// the time of a latency-bound kernel whose CTAs take the same time per plane,
+// two halo planes included.
+inline int bbpp_z_chunks(long long units, int nz, long long slots, int min_kz, int *kz) {
+  if (units < 1) units = 1;
+  if (slots < 1) slots = 1;
+  auto norm = [&](int nzc, int *k) {
+    int kk = (nz + nzc - 1) / nzc;
+    if (kk < min_kz && nz >= min_kz) kk = min_kz;
+    *k = kk;
+    return (nz + kk - 1) / kk;
+  };
+  long long c0 = slots / units;
+  if (c0 < 1) c0 = 1;
+  if (c0 > nz) c0 = nz;
+  int best = norm((int)c0, kz);
+  if ((double)units * best >= 0.9 * (double)slots) return best;
+  double tbest = 1e300;
+  for (int c = 1; c <= nz; c++) {
+    int k = 0;
+    const int cc = norm(c, &k);
+    if (cc != c) continue;
+    const long long waves = (units * cc + slots - 1) / slots;
+    const double t = (double)waves * (k + 2);
+    if (t < tbest) {
+      tbest = t;
+      best = cc;
+      *kz = k;
+    }
+  }
+  return best;
+}
+
 void bbpp_record_error(bbpp_ctx *ctx, cudaError_t e, const char *what, int line);
 int bbpp_geo_init(const bbpp_grid *g, bbpp::Geo *G);
 // profiling helpers (bbpp_solver.cu)

@@ -196,12 +196,9 @@ static void stencil_shape(bbpp_ctx *ctx) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_resid<double, double, true>, NT, 0);
   if (per_sm < 1) per_sm = 1;
-  const long long target = (long long)ctx->sms * per_sm;
-  int nzc = (int)std::max<long long>(1, target / std::max(1, gx * gy));
-  nzc = std::min(nzc, G.nz);
-  int kz = (G.nz + nzc - 1) / nzc;
-  if (kz < 4 && G.nz >= 4) kz = 4;  // keep the halo-plane overhead small
-  nzc = (G.nz + kz - 1) / kz;
+  // at least 4 planes per chunk keeps the halo-plane overhead small
+  int kz = 0;
+  const int nzc = bbpp_z_chunks((long long)gx * gy, G.nz, (long long)ctx->sms * per_sm, 4, &kz);
   ctx->kz = kz;
   ctx->sgrid = dim3(gx, gy, nzc);
   {
@@ -209,12 +206,8 @@ static void stencil_shape(bbpp_ctx *ctx) {
     int pf = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k_resid_s<double, double, true, true>, FNT, 0);
     if (pf < 1) pf = 1;
-    const long long tgt = (long long)ctx->sms * pf;
-    int nzf = (int)std::max<long long>(1, tgt / std::max(1, fx * fy));
-    nzf = std::min(nzf, G.nz);
-    int kzf = (G.nz + nzf - 1) / nzf;
-    if (kzf < 8 && G.nz >= 8) kzf = 8;
-    nzf = (G.nz + kzf - 1) / kzf;
+    int kzf = 0;
+    const int nzf = bbpp_z_chunks((long long)fx * fy, G.nz, (long long)ctx->sms * pf, 8, &kzf);
     ctx->fkz = kzf;
     ctx->fgrid = dim3(fx, fy, nzf);
   }
@@ -227,12 +220,8 @@ static void stencil_shape(bbpp_ctx *ctx) {
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k1_search2<float, true, true>, FNT, 0);
     if (pf < 1) pf = 1;
-    const long long tgt = (long long)ctx->sms * pf;
-    int nzf = (int)std::max<long long>(1, tgt / std::max(1, fx * fy));
-    nzf = std::min(nzf, G.nz);
-    int kzf = (G.nz + nzf - 1) / nzf;
-    if (kzf < 8 && G.nz >= 8) kzf = 8;
-    nzf = (G.nz + kzf - 1) / kzf;
+    int kzf = 0;
+    const int nzf = bbpp_z_chunks((long long)fx * fy, G.nz, (long long)ctx->sms * pf, 8, &kzf);
     ctx->pkz[prec] = kzf;
     ctx->pgrid[prec] = dim3(fx, fy, nzf);
   }

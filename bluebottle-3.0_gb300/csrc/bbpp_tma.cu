@@ -1194,11 +1194,14 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
   const int want = env_int("BBPP_TMA_NPT", 1);
   int ty;
   if (nx <= 256 && nx % 32 == 0) ty = (1024 / nx) * ((want == 2 || want == 4) ? want : 1);
-  else if (nx % 256 == 0 && nx <= 1024) ty = 4;
+  // wide rows (512 or 1024 floats): slabs of 2 rows, BBPP_TMA_TY=4 for 4.  At
+  // 512^3 a 4-row fused stage ring takes 147 KB, one CTA per SM; 2 rows take
+  // 98 KB, two per SM: 918 against 1005 us per fused launch
+  else if (nx % 256 == 0 && nx <= 1024) ty = env_int("BBPP_TMA_TY", 2) == 4 ? 4 : 2;
   else return;
   if (ny % ty != 0 || ty > 256) return;
   const int npt = ty * nx / 1024;
-  if (npt != 1 && npt != 2 && npt != 4) return;
+  if ((npt != 1 && npt != 2 && npt != 4) || npt * 1024 != ty * nx) return;
   const int stage = 2 * (ty + 2) * nx * 4;
   // 4 stages: one plane in flight beyond the three in use; more stages cost
   // resident CTAs (measured at 256^3: 4 CTAs/SM with 4 stages beat deeper rings)
@@ -1241,12 +1244,7 @@ void bbpp_tma_init(bbpp_ctx *ctx) {
   if (per_sm < 1) return;
   const int slabs = ny / ty;
   auto chunking = [&](int per, int *kz_out, dim3 *grid_out) {
-    const long long target = (long long)ctx->sms * per;
-    int nzc = (int)std::max<long long>(1, target / slabs);
-    nzc = std::min(nzc, nz);
-    const int kz = (nz + nzc - 1) / nzc;
-    nzc = (nz + kz - 1) / kz;
-    *kz_out = kz;
+    const int nzc = bbpp_z_chunks(slabs, nz, (long long)ctx->sms * per, 1, kz_out);
     *grid_out = dim3(slabs, nzc, 1);
   };
   chunking(per_sm, &t->kz, &t->grid);
