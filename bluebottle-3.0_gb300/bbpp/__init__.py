@@ -133,6 +133,7 @@ def lib():
         "bbpp_set_ff_resid": (I, [P, I]),
         "bbpp_set_xsum": (I, [P, I]),
         "bbpp_neighbour_sums": (I, [P, P, ctypes.c_longlong]),
+        "bbpp_plan_z_chunks": (I, [ctypes.c_longlong, I, ctypes.c_longlong, I, ctypes.POINTER(I)]),
         "bbpp_rng_uniform": (None, [ctypes.c_ulonglong, ctypes.c_longlong, D, D, P]),
         "bbpp_rng_gauss": (None, [ctypes.c_ulonglong, ctypes.c_longlong, P]),
         "bbpp_version": (ctypes.c_char_p, []),
@@ -381,6 +382,16 @@ def stream_mix_rate(cells):
     v = ctypes.c_double()
     _check(lib().bbpp_stream_mix_rate(int(cells), ctypes.byref(v)))
     return v.value
+
+
+def plan_z_chunks(units, nz, slots, min_kz):
+    """(z-chunks, planes per chunk) the stencil kernels launch with
+    (bbpp_plan_z_chunks; host arithmetic, no GPU needed)."""
+    kz = ctypes.c_int()
+    n = lib().bbpp_plan_z_chunks(int(units), int(nz), int(slots), int(min_kz), ctypes.byref(kz))
+    if n < 1:
+        raise BbppError(BAD_ARG, "plan_z_chunks")
+    return n, kz.value
 
 
 def neighbour_sums(v):

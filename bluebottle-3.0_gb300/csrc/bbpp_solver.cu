@@ -1308,6 +1308,11 @@ extern "C" int bbpp_fp64_fma_rate(double *fma_per_s) {
   return 0;
 }
 
+extern "C" int bbpp_plan_z_chunks(long long units, int nz, long long slots, int min_kz, int *kz) {
+  if (units < 1 || nz < 1 || slots < 1 || min_kz < 1 || !kz) return 0;
+  return bbpp_z_chunks(units, nz, slots, min_kz, kz);
+}
+
 // nb_sum6 over n six-tuples (the FP64 search kernel's interior neighbour sum)
 __global__ void k_nb_sum6(const double *__restrict__ in, double *__restrict__ out, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {

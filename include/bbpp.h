@@ -201,6 +201,13 @@ int bbpp_fp64_fma_rate(double *fma_per_s);
  * launches, the best kept).  Allocates its buffers (about 33 B per cell) for
  * the measurement.  No counterpart in the reference. */
 int bbpp_stream_mix_rate(long long cells, double *bytes_per_s);
+/* The z chunking the stencil kernels launch with (host arithmetic only): for
+ * `units` CTA columns (tiles or slabs) per plane, nz planes and `slots` CTAs
+ * resident at once, returns the number of z-chunks and sets *kz to the planes
+ * per chunk (at least min_kz where nz allows).  One wave of slots / units
+ * chunks when that fills at least 90% of the slots; otherwise the count that
+ * minimises waves x (kz + 2).  Returns 0 on bad arguments. */
+int bbpp_plan_z_chunks(long long units, int nz, long long slots, int min_kz, int *kz);
 /* out[i] = the FP64 search kernel's neighbour sum of in[6i .. 6i+5] (host
  * buffers, n <= 2^26): the fixed-point sum, or FP64 adds where all six are
  * zero or tiny or one is not finite.  For tests of that arithmetic. */
