@@ -465,9 +465,10 @@ def run_ours(args):
         return out
 
     def fp64_roof(name):
-        """The plain FP64 solve against the FP64 pipe it is bound by: FP64 thread
-        instructions of its kernels (per cell, from ncu) over their CUDA-event
-        time, against the FMA rate this GPU issues (bbpp_fp64_fma_rate)."""
+        """The plain FP64 solve against the FP64 pipe (1/64 of the FP32 rate on
+        this part; its update kernel is bound by it): FP64 thread instructions
+        of its kernels (per cell, from ncu) over their CUDA-event time, against
+        the FMA rate this GPU issues (bbpp_fp64_fma_rate)."""
         ks = res[name]["kstats"]
         if not ks or not fma_rate:
             return None
@@ -479,7 +480,7 @@ def run_ours(args):
         if ms == 0.0:
             return {"peak_fma_per_s": fma_rate, "unit": "FP64 inst/s"}
         achieved = inst / (ms * 1e-3)
-        return {"bound": "fp64 pipe", "achieved": achieved, "peak": fma_rate, "unit": "FP64 inst/s",
+        return {"resource": "fp64 pipe", "achieved": achieved, "peak": fma_rate, "unit": "FP64 inst/s",
                 "frac": achieved / fma_rate, "inst_per_cell": {k: v for k, v in NCU_FP64_INST.items()},
                 "kernels_ms_share": ms / sum(k[2] for k in ks), "peak_source": "bbpp_fp64_fma_rate (this run)"}
 

@@ -5,8 +5,9 @@
 // iteration needs no multiply for them.  With L x = S rhs the iterates are
 // those of the reference's PCG on (-A) x = rhs (alpha and beta are unchanged;
 // (r,z), (r,r) and (rhs,rhs) scale by S, S^2, S^2).  Scaling matters on GB300
-// because FP64 issues at ~1/58 of FP32: these kernels keep FP64 instructions
-// per cell to the stencil's adds, one FMA per update and one per dot.
+// because FP64 issues at 1/64 of FP32: these kernels keep FP64 instructions
+// per cell to one FMA per update, one per dot and one for the stencil, whose
+// six-neighbour sum runs on the integer pipe (xsum6) on isotropic grids.
 //
 // Cells of a solid sphere hold r = p = Ap = x = 0 throughout (their rhs is
 // taken as zero, as part_BC_p makes it, src/particle_kernel.cu:1753): the
