@@ -133,6 +133,7 @@ def lib():
         "bbpp_set_ff_resid": (I, [P, I]),
         "bbpp_set_xsum": (I, [P, I]),
         "bbpp_neighbour_sums": (I, [P, P, ctypes.c_longlong]),
+        "bbpp_neighbour_sums_host": (I, [P, P, ctypes.c_longlong]),
         "bbpp_plan_z_chunks": (I, [ctypes.c_longlong, I, ctypes.c_longlong, I, ctypes.POINTER(I)]),
         "bbpp_rng_uniform": (None, [ctypes.c_ulonglong, ctypes.c_longlong, D, D, P]),
         "bbpp_rng_gauss": (None, [ctypes.c_ulonglong, ctypes.c_longlong, P]),
@@ -394,13 +395,15 @@ def plan_z_chunks(units, nz, slots, min_kz):
     return n, kz.value
 
 
-def neighbour_sums(v):
+def neighbour_sums(v, host=False):
     """The FP64 search kernel's neighbour sum of each row of an (n, 6) float64
-    array, computed on the GPU (bbpp_neighbour_sums)."""
+    array, computed on the GPU (bbpp_neighbour_sums), or by the same code
+    compiled for the host (host=True, bbpp_neighbour_sums_host)."""
     v = np.ascontiguousarray(v, dtype=np.float64)
     assert v.ndim == 2 and v.shape[1] == 6
     out = np.empty(v.shape[0], np.float64)
-    _check(lib().bbpp_neighbour_sums(v.ctypes.data, out.ctypes.data, v.shape[0]))
+    fn = lib().bbpp_neighbour_sums_host if host else lib().bbpp_neighbour_sums
+    _check(fn(v.ctypes.data, out.ctypes.data, v.shape[0]))
     return out
 
 

@@ -26,6 +26,7 @@
 //             option).
 #pragma once
 
+#include <cstring>
 #include <type_traits>
 
 #include "bbpp_dev.cuh"
@@ -115,11 +116,41 @@ __device__ __forceinline__ T apply_L(const GeoL &G, const T *s_dL, int cls, T pc
 // to 1/2 ulp each for the FP64 adds.  Returns false, with `out` unset, when
 // the largest biased exponent lies outside [128, 2040] (all six zero or tiny,
 // or an Inf or NaN).
-__device__ __forceinline__ bool xsum6(const double (&v)[6], double &out) {
+// bit-level helpers of xsum6 on either side (the host copy serves the tests)
+__host__ __device__ __forceinline__ unsigned long long xs_bits(double d) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(d);
+#else
+  unsigned long long b;
+  memcpy(&b, &d, sizeof b);
+  return b;
+#endif
+}
+__host__ __device__ __forceinline__ double xs_double(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+__host__ __device__ __forceinline__ int xs_clz64(unsigned long long m) {  // m != 0
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)m);
+#else
+  return __builtin_clzll(m);
+#endif
+}
+
+__host__ __device__ __forceinline__ bool xsum6(const double (&v)[6], double &out) {
   // biased exponent << 20 of the largest magnitude
   unsigned int E = 0;
 #pragma unroll
-  for (int i = 0; i < 6; i++) E = max(E, (unsigned int)__double2hiint(v[i]) & 0x7ff00000u);
+  for (int i = 0; i < 6; i++) {
+    const unsigned int ei = (unsigned int)(xs_bits(v[i]) >> 32) & 0x7ff00000u;
+    E = E > ei ? E : ei;
+  }
   if (E < (128u << 20) || E > (2040u << 20)) return false;
   // A value of exponent field e shifts right by E - e + 4.  Zero and
   // subnormal values (e = 0) have no leading bit and lie below 2^-1022, under
@@ -128,13 +159,14 @@ __device__ __forceinline__ bool xsum6(const double (&v)[6], double &out) {
   long long acc = 0;
 #pragma unroll
   for (int i = 0; i < 6; i++) {
-    const unsigned int hi = (unsigned int)__double2hiint(v[i]), lo = (unsigned int)__double2loint(v[i]);
+    const unsigned long long bi = xs_bits(v[i]);
+    const unsigned int hi = (unsigned int)(bi >> 32), lo = (unsigned int)bi;
     const unsigned int raw = hi & 0x7ff00000u;
     // significand left-aligned in 64 bits: fraction at bits 62..11, the
     // leading bit (set iff the exponent field is non-zero) at bit 63
-    unsigned int whi = __funnelshift_l(lo, hi, 11);
+    unsigned int whi = (hi << 11) | (lo >> 21);
     whi = (whi & 0x7fffffffu) | ((raw + 0x7fffffffu) & 0x80000000u);
-    const unsigned int sh = min((Ep - raw) >> 20, 63u);
+    const unsigned int sh0 = (Ep - raw) >> 20, sh = sh0 < 63u ? sh0 : 63u;
     const long long w = (long long)((((unsigned long long)whi << 32) | (unsigned long long)(lo << 11)) >> sh);
     const long long sg = (long long)((int)hi >> 31);
     acc += (w ^ sg) - sg;
@@ -147,7 +179,7 @@ __device__ __forceinline__ bool xsum6(const double (&v)[6], double &out) {
     out = 0.0;
     return true;
   }
-  const int lz = __clzll((long long)m);  // >= 1: |acc| < 2^63
+  const int lz = xs_clz64(m);  // >= 1: |acc| < 2^63
   m <<= lz;
   const unsigned long long mant = m >> 11;  // 53 bits, leading bit at 52
   const unsigned int rest = (unsigned int)m & 0x7ffu;
@@ -155,14 +187,14 @@ __device__ __forceinline__ bool xsum6(const double (&v)[6], double &out) {
   // biased exponent E + 4 - lz, of which the leading bit of mant adds one; a
   // carry out of the rounding adds another
   const unsigned long long bits = ((unsigned long long)((E >> 20) + 3u - (unsigned int)lz) << 52) + mant + up;
-  out = __longlong_as_double((long long)(bits | ((unsigned long long)sg & 0x8000000000000000ull)));
+  out = xs_double(bits | ((unsigned long long)sg & 0x8000000000000000ull));
   return true;
 }
 
 // The isotropic neighbour sum of FP64 p: xsum6 where it applies, FP64 adds in
 // the stencil's order otherwise.  A solid cell (`skip`) discards its result, so
 // it never takes the FP64 branch.
-__device__ __forceinline__ double nb_sum6(double pe, double pw, double pn, double ps, double pt, double pb,
+__host__ __device__ __forceinline__ double nb_sum6(double pe, double pw, double pn, double ps, double pt, double pb,
                                           bool skip) {
   const double v[6] = {pe, pw, pn, ps, pt, pb};
   double s;

@@ -1321,6 +1321,15 @@ __global__ void k_nb_sum6(const double *__restrict__ in, double *__restrict__ ou
   }
 }
 
+extern "C" int bbpp_neighbour_sums_host(const double *in, double *out, long long n) {
+  if (n < 0 || (n > 0 && (!in || !out))) return BBPP_BAD_ARG;
+  for (long long i = 0; i < n; i++) {
+    const double *v = in + 6 * i;
+    out[i] = nb_sum6(v[0], v[1], v[2], v[3], v[4], v[5], false);
+  }
+  return 0;
+}
+
 extern "C" int bbpp_neighbour_sums(const double *in, double *out, long long n) {
   bbpp_ctx *ctx = nullptr;
   if (n < 0 || (n > 0 && (!in || !out)) || n > (1ll << 26)) return BBPP_BAD_ARG;

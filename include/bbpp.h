@@ -212,6 +212,8 @@ int bbpp_plan_z_chunks(long long units, int nz, long long slots, int min_kz, int
  * buffers, n <= 2^26): the fixed-point sum, or FP64 adds where all six are
  * zero or tiny or one is not finite.  For tests of that arithmetic. */
 int bbpp_neighbour_sums(const double *in, double *out, long long n);
+/* The same arithmetic compiled for the host, on host buffers (no GPU). */
+int bbpp_neighbour_sums_host(const double *in, double *out, long long n);
 /* Page-locked host memory (for end-to-end timing from pinned buffers). */
 int bbpp_host_alloc(size_t bytes, void **ptr);
 int bbpp_host_free(void *ptr);

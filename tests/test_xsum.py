@@ -4,9 +4,10 @@ bluebottle-3.0_gb300/csrc/bbpp_fast.cuh).
 The plain FP64 iteration adds each interior cell's six neighbours as one
 fixed-point sum on the integer pipe instead of five FP64 adds.  `model` below
 restates that arithmetic with Python integers.  The CPU tests hold the model to
-its stated bound against exact rational sums and compare it with the FP64 adds
-it replaces; the GPU tests hold the library's kernel bit-exact to the model and
-run whole solves with the sum on and off.
+its stated bound against exact rational sums, compare it with the FP64 adds it
+replaces, and hold the same C++ compiled for the host bit-exact to it; the GPU
+tests hold the library's kernel bit-exact to the model and run whole solves
+with the sum on and off.
 """
 import os
 import struct
@@ -138,16 +139,40 @@ def test_model_edge_cases():
     assert model([big] * 6) == (6 * big, 2023)
 
 
+EDGE_ROWS = [[1.0, 0, 0, 0, 0, 0], [0.0] * 6, [-0.0] * 6, [np.inf, 1, 0, 0, 0, 0], [np.nan, 1, 2, 3, 4, 5],
+             [1.0, 2.0 ** -53, 2.0 ** -53, 0, 0, 0], [2.0 ** 1000] * 6, [1e-310, -3e-310, 0, 0, 0, 1e-300]]
+
+
+def _same_bits(got, want):
+    return (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+
+
+def test_host_build_matches_model():
+    """The C++ of the kernel's sum, compiled for the host (the library's
+    bbpp_neighbour_sums_host), bit for bit against the model."""
+    import bbpp
+    try:
+        bbpp.lib()
+    except OSError as e:
+        pytest.skip(str(e))
+    v = sample(20000, 4)
+    v[:len(EDGE_ROWS)] = EDGE_ROWS
+    got = bbpp.neighbour_sums(v, host=True)
+    want = np.array([model(row)[0] for row in v])
+    same = _same_bits(got, want)
+    assert same.all(), np.flatnonzero(~same)[:10]
+
+
 @pytest.mark.gpu
 def test_gpu_neighbour_sums_match_model():
     import bbpp
     v = sample(20000, 3)
-    v[:8] = [[1.0, 0, 0, 0, 0, 0], [0.0] * 6, [-0.0] * 6, [np.inf, 1, 0, 0, 0, 0], [np.nan, 1, 2, 3, 4, 5],
-             [1.0, 2.0 ** -53, 2.0 ** -53, 0, 0, 0], [2.0 ** 1000] * 6, [1e-310, -3e-310, 0, 0, 0, 1e-300]]
+    v[:len(EDGE_ROWS)] = EDGE_ROWS
     got = bbpp.neighbour_sums(v)
     want = np.array([model(row)[0] for row in v])
-    same = (got.view(np.uint64) == want.view(np.uint64)) | (np.isnan(got) & np.isnan(want))
+    same = _same_bits(got, want)
     assert same.all(), np.flatnonzero(~same)[:10]
+    assert _same_bits(got, bbpp.neighbour_sums(v, host=True)).all()
 
 
 @pytest.mark.gpu
