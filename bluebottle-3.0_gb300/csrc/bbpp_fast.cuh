@@ -732,7 +732,7 @@ __device__ __forceinline__ void resid_finish(DevState *st, const double (&tot)[3
 // solid cells.  TXT: type of x and rhs, TR: type of r.  Dots in FP64 of the
 // stored r: (r,z), (r,r); and (rhs,rhs) of the unscaled rhs.
 template <typename TXT, typename TR, bool MASK, bool ISO>
-__global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__ xin, const TXT *__restrict__ rhs,
+__global__ void __launch_bounds__(FNT, 3) k_resid_s(const GeoL G, TXT *__restrict__ xin, const TXT *__restrict__ rhs,
                                                  TR *__restrict__ rout, const uint8_t *__restrict__ mask,
                                                  DevState *st, double *partials, int kz, int mode, double bscale) {
   __shared__ TXT s_dL[27], s_inv[27];
@@ -749,20 +749,46 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
   const int nx = G.nx, ny = G.ny, nz = G.nz;
   const long long sxy = (long long)nx * ny;
   __syncthreads();
-  auto load_plane = [&](int slot, int zr) {
-    const int gz = halo_index(zr, nz, G.pz);
-    for (int e = tid; e < FHE; e += FNT) {
+  // The x tile of a plane plus halo is loaded into registers one plane ahead
+  // (issue) and written to shared memory the next plane (commit), so the
+  // loads are in flight while a plane is computed.  Per element: its offset in
+  // a plane (-1 outside a wall) and its places in the two tiles.
+  int eoff[FPER], epos[FPER], mpos[FPER];
+#pragma unroll
+  for (int k = 0; k < FPER; k++) {
+    const int e = tid + k * FNT;
+    eoff[k] = -1;
+    epos[k] = -1;
+    mpos[k] = 0;
+    if (e < FHE) {
       const int ly = e / FHX, lx = e - ly * FHX;
-      const int gx = halo_index(x0 + lx - 1, nx, G.px), gy = halo_index(y0 + ly - 1, ny, G.py);
-      TXT val = TXT(0);
-      uint8_t m = 0;
-      if (gz >= 0 && gx >= 0 && gy >= 0) {
-        const long long c = gx + (long long)nx * gy + sxy * gz;
-        if (MASK) m = mask[c];
-        val = m ? TXT(0) : xin[c];  // solid cells count as x = 0
+      epos[k] = e;
+      mpos[k] = ly * (FHX + 2) + lx;
+      const int hx = halo_index(x0 + lx - 1, nx, G.px), hy = halo_index(y0 + ly - 1, ny, G.py);
+      if (hx >= 0 && hy >= 0) eoff[k] = hx + nx * hy;
+    }
+  }
+  TXT pv[FPER];
+  uint8_t pm[FPER];
+  auto issue = [&](int zr) {
+    const int gz = halo_index(zr, nz, G.pz);
+#pragma unroll
+    for (int k = 0; k < FPER; k++) {
+      pv[k] = TXT(0);
+      pm[k] = 0;
+      if (gz >= 0 && eoff[k] >= 0) {
+        const long long c = eoff[k] + sxy * gz;
+        if (MASK) pm[k] = mask[c];
+        pv[k] = xin[c];
       }
-      sp[slot][ly][lx] = val;
-      sm[slot][ly][lx] = m;
+    }
+  };
+  auto commit = [&](int slot) {
+#pragma unroll
+    for (int k = 0; k < FPER; k++) {
+      if (epos[k] < 0) continue;
+      (&sp[slot][0][0])[epos[k]] = pm[k] ? TXT(0) : pv[k];  // solid cells count as x = 0
+      (&sm[slot][0][0])[mpos[k]] = pm[k];
     }
   };
   // (r,z) = (r,r) + sum over wall cells of (invL - 1) r^2; (rhs,rhs) only
@@ -770,10 +796,21 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
   // no predicated work on interior planes (FP64 issues at 1/64 of FP32).
   double corr = 0, rr = 0, bb = 0;
   const bool want_bb = mode == 0;
-  load_plane(0, z0 - 1);
-  load_plane(1, z0);
+  issue(z0 - 1);
+  commit(0);
+  issue(z0);
+  commit(1);
+  issue(z0 + 1);
   const int gx = x0 + tx;
-  auto cell = [&](auto interior_tag, int sb, int sc, int st_, int z) {
+  // rhs of the thread's own cells of a plane, loaded one plane ahead
+  auto load_b = [&](int z, TXT (&b)[2]) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int gy = y0 + ty + 8 * h;
+      b[h] = (gx < nx && gy < ny) ? rhs[gx + (long long)nx * gy + sxy * z] : TXT(0);
+    }
+  };
+  auto cell = [&](auto interior_tag, int sb, int sc, int st_, int z, const TXT (&bz)[2]) {
     constexpr bool INTERIOR = decltype(interior_tag)::value;
 #pragma unroll
     for (int h = 0; h < 2; h++) {
@@ -782,7 +819,7 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       const int ly = ty + 1 + 8 * h, lx = tx + 1;
       const bool mc = MASK && sm[sc][ly][lx] != 0;
       const long long c = gx + (long long)nx * gy + sxy * z;
-      const TXT bv = rhs[c];
+      const TXT bv = bz[h];
       if (want_bb) bb = fma((double)bv, (double)bv, bb);
       if (mc) {
         rout[c] = TR(0);
@@ -809,13 +846,19 @@ __global__ void __launch_bounds__(FNT) k_resid_s(const GeoL G, TXT *__restrict__
       }
     }
   };
+  TXT bcur[2] = {TXT(0), TXT(0)}, bnext[2] = {TXT(0), TXT(0)};
+  if (z0 < z1) load_b(z0, bcur);
   for (int z = z0; z < z1; z++) {
     const int sb = (z - z0) % 3, sc = (z - z0 + 1) % 3, st_ = (z - z0 + 2) % 3;
-    load_plane(st_, z + 1);
+    commit(st_);  // plane z + 1, loaded during the previous plane
+    if (z + 2 <= z1) issue(z + 2);
+    if (z + 1 < z1) load_b(z + 1, bnext);
     __syncthreads();
-    if (G.px && G.py && wall_count(z, nz, G.pz) == 0) cell(std::true_type(), sb, sc, st_, z);
-    else cell(std::false_type(), sb, sc, st_, z);
+    if (G.px && G.py && wall_count(z, nz, G.pz) == 0) cell(std::true_type(), sb, sc, st_, z, bcur);
+    else cell(std::false_type(), sb, sc, st_, z, bcur);
     __syncthreads();
+    bcur[0] = bnext[0];
+    bcur[1] = bnext[1];
   }
   double v[3] = {rr + corr, rr, bb}, tot[3];
   const unsigned int nb = gridDim.x * gridDim.y * gridDim.z;
