@@ -117,6 +117,20 @@ __device__ __forceinline__ unsigned int ld_u32_pol(const void *a, unsigned long 
   return v;
 }
 
+// FP32 -> FP64, exact, with integer operations: GB300 runs the conversion
+// instruction on the FP64 pipe (1/64 of the FP32 rate).  Zero keeps its sign;
+// subnormal inputs (never produced by the solver's vectors in practice) take
+// the conversion instruction.
+__device__ __forceinline__ double widen_f32(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned int e32 = (u >> 23) & 0xffu;
+  const unsigned long long frac = (unsigned long long)(u & 0x7fffffu) << 29;
+  if (e32 == 0) return frac ? (double)f : __longlong_as_double((long long)sign);
+  if (e32 == 0xffu) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull | frac));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e32 - 127u + 1023u) << 52) | frac));
+}
+
 __device__ __forceinline__ unsigned int fdiv(unsigned int n, unsigned long long m) {
   return m ? (unsigned int)__umul64hi((unsigned long long)n, m) : n;
 }

@@ -47,11 +47,12 @@ void bbpp_ir_free(bbpp_ctx *ctx) {
   ctx->ir = nullptr;
 }
 
-// x += d (FP64 accumulation of the FP32 correction)
+// x += d (FP64 accumulation of the FP32 correction, widened exactly with
+// integer operations)
 __global__ void k_add_correction(const Geo G, double *__restrict__ x, const float *__restrict__ d) {
   const unsigned int n = (unsigned int)G.n;
   for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-    x[c] += (double)d[c];
+    x[c] += widen_f32(d[c]);
 }
 
 static int ensure_ir(bbpp_ctx *ctx);

@@ -547,7 +547,8 @@ void bbpp_set_reliable(double *xhi, const double *rhs) {
 }
 
 // Reliable update of the mixed-precision solve: x_hi += d (+ alpha p when d
-// lags), d = 0, all in FP64.  check as for k_settle.
+// lags), d = 0, all in FP64; d and p are widened with integer operations, so
+// the FP64 pipe sees only the add and the FMA.  check as for k_settle.
 __global__ void __launch_bounds__(FNT) k_fold(const GeoL G, double *__restrict__ xhi, float *__restrict__ d,
                                               const float *__restrict__ p, const DevState *st, int check) {
   pdl_sync();
@@ -556,8 +557,8 @@ __global__ void __launch_bounds__(FNT) k_fold(const GeoL G, double *__restrict__
   const double alpha = lag ? *(volatile const double *)&st->alpha : 0.0;
   const unsigned int n = (unsigned int)G.n;
   for (unsigned int c = blockIdx.x * FNT + threadIdx.x; c < n; c += gridDim.x * FNT) {
-    double v = xhi[c] + (double)d[c];
-    if (lag) v = fma(alpha, (double)p[c], v);
+    double v = xhi[c] + widen_f32(d[c]);
+    if (lag) v = fma(alpha, widen_f32(p[c]), v);
     xhi[c] = v;
     d[c] = 0.f;
   }
