@@ -132,6 +132,8 @@ def lib():
         "bbpp_set_fused": (I, [P, I]),
         "bbpp_set_ff_resid": (I, [P, I]),
         "bbpp_set_xsum": (I, [P, I]),
+        "bbpp_set_trace": (I, [P, I]),
+        "bbpp_get_trace": (I, [P, P, P, I]),
         "bbpp_neighbour_sums": (I, [P, P, ctypes.c_longlong]),
         "bbpp_neighbour_sums_host": (I, [P, P, ctypes.c_longlong]),
         "bbpp_plan_z_chunks": (I, [ctypes.c_longlong, I, ctypes.c_longlong, I, ctypes.POINTER(I)]),
@@ -328,6 +330,18 @@ class Solver:
         kernel, the FP64 residuals): interior neighbour sums as exact
         fixed-point sums on the integer pipe (True) or FP64 adds."""
         _check(lib().bbpp_set_xsum(self.handle, 1 if on else 0))
+
+    def set_trace(self, n):
+        """Record alpha_k, beta_k of the first n iterations of later plain FP64 solves."""
+        _check(lib().bbpp_set_trace(self.handle, int(n)))
+        self._trace_n = int(n)
+
+    def trace(self):
+        """(alpha, beta) of the last plain FP64 solve (NaN past its end)."""
+        n = getattr(self, "_trace_n", 0)
+        a, b = np.empty(n), np.empty(n)
+        _check(lib().bbpp_get_trace(self.handle, a.ctypes.data, b.ctypes.data, n))
+        return a, b
 
     def kernel_stats(self):
         arr = (KStat * 32)()

@@ -63,7 +63,16 @@ struct DevState {
   int inject;            // test hook: 1 = the first TMA search CTA skips the copies of one plane
   long long wait_ns;     // bound of a device-side wait (0: one second)
   int fq;                // fused iteration kernels completed in this solve
+  // alpha_k and beta_k of iterations 1 .. trace_n (index k - 1), recorded by
+  // the search kernel (k1_search2) and the end of an iteration; null: none
+  double *trace_a;
+  double *trace_b;
+  int trace_n;
 };
+
+__device__ __forceinline__ void trace_put(double *buf, int n, int i, double v) {
+  if (buf && i >= 0 && i < n) buf[i] = v;
+}
 
 // Set by the last CTA of a search kernel: does this iteration's checkpoint
 // (if it is one) replace the residual?
@@ -236,6 +245,7 @@ __device__ __forceinline__ void finish_iteration(DevState *st, double rz1, doubl
     st->done = DONE_NAN;
   } else {
     st->beta = rz1 / st->rz;
+    trace_put(st->trace_b, st->trace_n, it - 1, st->beta);
     st->rz = rz1;
     if (it > st->max_iter) st->done = DONE_MAX_ITER;
   }

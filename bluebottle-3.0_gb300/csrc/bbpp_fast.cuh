@@ -501,6 +501,7 @@ __global__ void __launch_bounds__(FNT, sizeof(T) == 8 ? 3 : 4) k1_search2(const 
   if (last_cta_reduce<1>(v, partials, st, nb, bid, s_red, tot) && tid == 0) {
     st->pAp = tot[0];
     st->alpha = st->rz / tot[0];
+    trace_put(st->trace_a, st->trace_n, st->iter, st->alpha);
     st->first = 0;
     st->dlag = 1;
     decide_replacement(st);

@@ -96,6 +96,8 @@ struct bbpp_ctx {
   bool ff_resid = false;          // FP64 x -> FP32 r residuals in float-float arithmetic (else FP64)
   int inject = 0;                 // test hook of bbpp_debug_wait (see DevState::inject)
   long long wait_ns = 0;          // bound of device-side waits (0: one second)
+  double *trace = nullptr;        // alpha / beta trace of the next solves (2 * trace_n doubles), or null
+  int trace_n = 0;
 };
 
 // Launch an iteration kernel on ctx->stream; with ctx->pdl it may start while

@@ -327,6 +327,7 @@ extern "C" int bbpp_destroy(bbpp_ctx *ctx) {
   bbpp_net_ctx_free(ctx);
   bbpp_tma_free(ctx);
   if (ctx->st) cudaFree(ctx->st);
+  if (ctx->trace) cudaFree(ctx->trace);
   if (ctx->partials) cudaFree(ctx->partials);
   if (ctx->r) cudaFree(ctx->r);
   if (ctx->p[0]) cudaFree(ctx->p[0]);
@@ -903,6 +904,13 @@ int bbpp_pcg_init(bbpp_ctx *ctx, const uint8_t *mask, const T *rhs, T *x, T *r, 
   hst->wait_ns = ctx->wait_ns;
   hst->stop = stop;
   hst->first = 1;
+  if (ctx->trace && sizeof(T) == 8) {
+    // the plain FP64 method's alpha and beta; entries not reached stay NaN
+    hst->trace_a = ctx->trace;
+    hst->trace_b = ctx->trace + ctx->trace_n;
+    hst->trace_n = ctx->trace_n;
+    CK(cudaMemsetAsync(ctx->trace, 0xff, sizeof(double) * 2 * (size_t)ctx->trace_n, ctx->stream));
+  }
   CK(cudaMemcpyAsync(st, hst, sizeof(DevState), cudaMemcpyHostToDevice, ctx->stream));
   if (zero_x) CK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)ctx->G.n, ctx->stream));
   bbpp_launch_resid_s<T, T>(ctx, mask, x, rhs, r, st, RES_INIT, bscale);
@@ -1475,6 +1483,28 @@ extern "C" int bbpp_set_ff_resid(bbpp_ctx *ctx, int on) {
   if (!ctx || (on != 0 && on != 1)) return BBPP_BAD_ARG;
   ctx->ff_resid = on == 1;
   drop_graphs(ctx);  // the replacement kernels are captured in the iteration graphs
+  return 0;
+}
+
+extern "C" int bbpp_set_trace(bbpp_ctx *ctx, int n) {
+  if (!ctx || n < 0 || n > (1 << 20)) return BBPP_BAD_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->trace) CK(cudaFree(ctx->trace));
+  ctx->trace = nullptr;
+  ctx->trace_n = 0;
+  if (n > 0) {
+    CK(cudaMalloc(&ctx->trace, sizeof(double) * 2 * (size_t)n));
+    ctx->trace_n = n;
+  }
+  return 0;
+}
+
+extern "C" int bbpp_get_trace(bbpp_ctx *ctx, double *alpha, double *beta, int n) {
+  if (!ctx || n < 0 || n > ctx->trace_n || (n > 0 && (!alpha || !beta))) return BBPP_BAD_ARG;
+  if (n == 0) return 0;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(alpha, ctx->trace, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(beta, ctx->trace + ctx->trace_n, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost));
   return 0;
 }
 

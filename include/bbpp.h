@@ -246,6 +246,12 @@ int bbpp_set_ff_resid(bbpp_ctx *ctx, int on);
  * 0 = five FP64 adds.  No counterpart in the reference, whose stencil adds in
  * FP64 (src/solver_kernel.cu:691-707). */
 int bbpp_set_xsum(bbpp_ctx *ctx, int on);
+/* Record alpha_k and beta_k of the first n iterations of the following plain
+ * FP64 solves (n = 0: stop; at most 2^20); bbpp_get_trace copies them out,
+ * NaN where a solve ended earlier.  For comparing the iteration with the
+ * reference's (src/cuda_solver.cu:205-243); no counterpart there. */
+int bbpp_set_trace(bbpp_ctx *ctx, int n);
+int bbpp_get_trace(bbpp_ctx *ctx, double *alpha, double *beta, int n);
 
 /* ---- learned initial guess (no counterpart in the reference) ----
  * A 3-level 3D conv encoder-decoder (channels 16/32/64, 3x3x3 kernels, BF16

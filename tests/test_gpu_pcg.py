@@ -292,3 +292,28 @@ def test_ws_fused_kernel_matches_fused(lib, name, n, bc, ws_ns, monkeypatch):
     if mask is None:
         x0, x1 = x0 - x0.mean(), x1 - x1.mean()
     assert np.abs(x0 - x1).max() <= 1e-5 * np.abs(x0).max()
+
+
+@pytest.mark.parametrize("xsum", [True, False])
+@pytest.mark.parametrize("name,n", [("C1", 32), ("C2", 48)])
+def test_alpha_beta_trace_matches_oracle(lib, orc, name, n, xsum):
+    """The iteration itself against the oracle's PCG on the same inputs:
+    alpha_k and beta_k of the first 50 iterations of the plain FP64 method
+    agree to 1e-12 relative, with the six-neighbour sums on the integer pipe
+    and with FP64 adds.  (The library iterates on the scaled operator, whose
+    alpha and beta are the reference's.)"""
+    g, mask, rhs, _ = problems.make_problem(name, n=n)
+    s = bbpp.Solver(g)
+    s.set_xsum(xsum)
+    s.set_trace(50)
+    x, rep = s.solve_host(rhs, mask, tol=1e-13)
+    a, b = s.trace()
+    xo, res = orc.pcg(to_orc(orc, g), rhs, mask, tol=1e-13, trace=50)
+    assert rep.iters > 50 and res["iters"] > 50
+    assert np.isfinite(a).all() and np.isfinite(b).all()
+    ra = np.abs(a - res["alpha"]) / np.abs(res["alpha"])
+    rb = np.abs(b - res["beta"]) / np.abs(res["beta"])
+    assert ra.max() <= 1e-12 and rb.max() <= 1e-12, (ra.max(), rb.max())
+    # a later solve without the trace leaves the recorded values alone
+    s.set_trace(0)
+    s.solve_host(rhs, mask, tol=1e-8)
