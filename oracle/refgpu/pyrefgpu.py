@@ -40,6 +40,7 @@ def lib():
         L.refgpu_set_cubin.argtypes = [P, ctypes.c_size_t]
         L.refgpu_setup.argtypes = [I, I, I, D, D, D, P, P]
         L.refgpu_solve.argtypes = [P, D, I, P, ctypes.POINTER(I), ctypes.POINTER(D), ctypes.POINTER(D)]
+        L.refgpu_set_trace.argtypes = [P, P, I]
         L.refgpu_error.restype = ctypes.c_char_p
         L.refgpu_cages_set_cubin.argtypes = [P, ctypes.c_size_t]
         L.refgpu_cages_setup.argtypes = [I, I, I, D, D, D, P]
@@ -75,16 +76,25 @@ class RefSolver:
             raise RuntimeError("refgpu_setup %d: %s" % (rc, L.refgpu_error().decode()))
         self.shape = (nz, ny, nx)
 
-    def solve(self, rhs, residual, max_iter=20000):
-        """rhs: the reference's -b (dense); returns (phi, niter, resid, ms, status)."""
+    def solve(self, rhs, residual, max_iter=20000, trace=0):
+        """rhs: the reference's -b (dense); returns (phi, niter, resid, ms, status),
+        and with trace > 0 also (alpha, beta) of its first `trace` iterations (NaN
+        past the last)."""
         L = lib()
         rhs = np.ascontiguousarray(rhs, dtype=np.float64)
         phi = np.empty(self.shape, np.float64)
         it, res, ms = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
-        rc = L.refgpu_solve(rhs.ctypes.data, residual, max_iter, phi.ctypes.data, ctypes.byref(it), ctypes.byref(res),
-                            ctypes.byref(ms))
+        ta, tb = np.full(max(trace, 1), np.nan), np.full(max(trace, 1), np.nan)
+        L.refgpu_set_trace(ta.ctypes.data if trace else None, tb.ctypes.data if trace else None, trace)
+        try:
+            rc = L.refgpu_solve(rhs.ctypes.data, residual, max_iter, phi.ctypes.data, ctypes.byref(it),
+                                ctypes.byref(res), ctypes.byref(ms))
+        finally:
+            L.refgpu_set_trace(None, None, 0)
         if rc not in (0, 11, 12):
             raise RuntimeError("refgpu_solve %d: %s" % (rc, L.refgpu_error().decode()))
+        if trace:
+            return phi, it.value, res.value, ms.value, rc, (ta[:trace].copy(), tb[:trace].copy())
         return phi, it.value, res.value, ms.value, rc
 
     def close(self):

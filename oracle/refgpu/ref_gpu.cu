@@ -397,6 +397,15 @@ int refgpu_setup(int nx, int ny, int nz, double dx, double dy, double dz, const 
 // NULL); niter, resid (sqrt((r,z)/(b,b)) at exit) and ms (CUDA events around
 // the whole solve, from the rhs reset to the last check) out.  Returns 0, or
 // 11 on a NaN residual, 12 when max_iter is exceeded (the reference exits).
+// alpha_k and beta_k of the next solves, iterations 1 .. n (host arrays; NULL: none)
+static double *g_trace_a = nullptr, *g_trace_b = nullptr;
+static int g_trace_n = 0;
+void refgpu_set_trace(double *alpha, double *beta, int n) {
+  g_trace_a = alpha;
+  g_trace_b = beta;
+  g_trace_n = (alpha && beta && n > 0) ? n : 0;
+}
+
 int refgpu_solve(const double *rhs, double residual, int max_iter, double *phi, int *niter, double *resid,
                  double *ms) {
   Ref *R = g_ref;
@@ -446,6 +455,7 @@ int refgpu_solve(const double *rhs, double residual, int max_iter, double *phi, 
       }
       const double DENOM = dot(R->p, R->Ap, R->s3);
       double alpha = sp_rq / DENOM;
+      if (q - 1 < g_trace_n) g_trace_a[q - 1] = alpha;
       if (q % 50 == 0) {
         void *a1[] = {&R->phi, &R->p, &alpha};
         launch(R, R->f_solution, R->kn, a1);
@@ -467,6 +477,7 @@ int refgpu_solve(const double *rhs, double residual, int max_iter, double *phi, 
         break;
       } else {
         double beta = sp_rq1 / sp_rq;
+        if (q - 1 < g_trace_n) g_trace_b[q - 1] = beta;
         void *a[] = {&R->p, &R->pb, &R->z, &beta};
         launch(R, R->f_search, R->kn, a);
         exchange<double>(R, R->pb);

@@ -59,6 +59,27 @@ def test_library_matches_reference_gpu(bbpp_lib, name, n, tol):
         np.linalg.norm(x - phi) <= 1e-6 * np.linalg.norm(phi)
 
 
+@pytest.mark.parametrize("name,n", [("C1", 32), ("C2", 64)])
+def test_alpha_beta_trace_matches_reference_gpu(bbpp_lib, name, n):
+    """alpha_k and beta_k of the first 50 iterations of this library's FP64
+    PCG against those of the reference's own CUDA PCG (its unmodified kernels
+    under the restated one-rank loop) on identical inputs: 1e-12 relative."""
+    g, mask, rhs, _ = problems.make_problem(name, n=n)
+    bc = tuple(int(v) for v in g.bc)
+    ref = pyrefgpu.RefSolver(g.nx, g.ny, g.nz, g.dx, g.dy, g.dz, bc, mask)
+    phi, it, res, ms, rc, (ra, rb) = ref.solve(rhs, 1e-12, trace=50)
+    ref.close()
+    assert rc == 0 and it > 50
+    s = bbpp.Solver(g)
+    s.set_trace(50)
+    x, rep = s.solve_host(rhs, mask, tol=1e-12, stop=bbpp.STOP_REF_RZ)
+    a, b = s.trace()
+    assert rep.status == bbpp.CONVERGED
+    da = np.abs(a - ra) / np.abs(ra)
+    db = np.abs(b - rb) / np.abs(rb)
+    assert da.max() <= 1e-12 and db.max() <= 1e-12, (da.max(), db.max())
+
+
 def full_size_inputs(name):
     """The stated workloads at their full sizes: C2 = 128^3, 64 spheres of
     radius 8 cells, spectral RHS; C3 = 256^3, 1000 spheres of radius 6 cells,
