@@ -101,21 +101,6 @@ __device__ __forceinline__ T apply_L(const GeoL &G, const T *s_dL, int cls, T pc
 }
 
 // ---------------------------------------------- exact neighbour sums ---
-// The six-neighbour sum of the isotropic stencil in FP64 as one fixed-point
-// sum on the integer pipe, rounded once to nearest even.  GB300 issues FP64 at
-// 1/64 of its FP32 rate, and the five FP64 adds kept the FP64 search kernel on
-// that pipe; the ~150 integer operations below run beside the remaining FP64
-// work (at 256^3 the kernel went from 370 to 311 us per launch).
-//
-// Each 53-bit significand is aligned to the largest exponent of the six, the
-// largest value's leading bit at bit 59 of a signed 64-bit accumulator; bits
-// shifted below bit 0 are dropped, under one unit (2^-59 of the largest
-// value's leading bit) per value.  Six aligned magnitudes stay below 6 * 2^60
-// < 2^63, so the accumulator cannot overflow.  The result lies within 1/2 ulp
-// of the exact sum plus six units (ulp(max)/128), against five roundings of up
-// to 1/2 ulp each for the FP64 adds.  Returns false, with `out` unset, when
-// the largest biased exponent lies outside [128, 2040] (all six zero or tiny,
-// or an Inf or NaN).
 // bit-level helpers of xsum6 on either side (the host copy serves the tests)
 __host__ __device__ __forceinline__ unsigned long long xs_bits(double d) {
 #ifdef __CUDA_ARCH__
@@ -143,6 +128,21 @@ __host__ __device__ __forceinline__ int xs_clz64(unsigned long long m) {  // m !
 #endif
 }
 
+// The six-neighbour sum of the isotropic stencil in FP64 as one fixed-point
+// sum on the integer pipe, rounded once to nearest even.  GB300 issues FP64 at
+// 1/64 of its FP32 rate, and the five FP64 adds kept the FP64 search kernel on
+// that pipe; the ~150 integer operations below run beside the remaining FP64
+// work (at 256^3 the kernel went from 370 to 311 us per launch).
+//
+// Each 53-bit significand is aligned to the largest exponent of the six, the
+// largest value's leading bit at bit 59 of a signed 64-bit accumulator; bits
+// shifted below bit 0 are dropped, under one unit (2^-59 of the largest
+// value's leading bit) per value.  Six aligned magnitudes stay below 6 * 2^60
+// < 2^63, so the accumulator cannot overflow.  The result lies within 1/2 ulp
+// of the exact sum plus six units (ulp(max)/128), against five roundings of up
+// to 1/2 ulp each for the FP64 adds.  Returns false, with `out` unset, when
+// the largest biased exponent lies outside [128, 2040] (all six zero or tiny,
+// or an Inf or NaN).
 __host__ __device__ __forceinline__ bool xsum6(const double (&v)[6], double &out) {
   // biased exponent << 20 of the largest magnitude
   unsigned int E = 0;
