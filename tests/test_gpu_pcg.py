@@ -344,3 +344,24 @@ def test_anisotropic_solves_match_oracle(lib, orc, dims, spacing, bc):
     x32, r32 = s.solve_host(rhs, mask, tol=1e-9, precision=bbpp.FP32_IR)
     assert r32.status == bbpp.CONVERGED and r32.true_rel <= 1e-9 * 1.01
     assert np.abs(x32 - xo).max() <= 100 * 1e-9 * np.abs(xo).max()
+
+
+@pytest.mark.parametrize("dims", [(1024, 32, 12), (768, 16, 10), (512, 24, 9)])
+def test_wide_row_fp32_paths_match_oracle(lib, orc, dims):
+    """Rows of 512 and 1024 cells take the TMA kernels on 2-row slabs through
+    4-D tensor maps (1024: two float4 per thread and plane); 768 cells take the
+    z-marching kernels.  The FP32 method with FP64 reliable updates to 1e-9
+    against the oracle's FP64 PCG to 1e-13."""
+    nx, ny, nz = dims
+    g = bbpp.Grid.make(nx, ny, nz, 1.0 / nx, 1.0 / nx, 1.0 / nx, (P, P, P, P, N, N))
+    mask = rand_mask(g.shape, nx, 0.05)
+    rng = np.random.default_rng(nz)
+    rhs = rng.normal(size=g.shape)
+    rhs[mask == 1] = 0
+    s = bbpp.Solver(g)
+    xo, res = orc.pcg(to_orc(orc, g), rhs, mask, tol=1e-13)
+    assert res["status"] == 0
+    x, rep = s.solve_host(rhs, mask, tol=1e-9, precision=bbpp.FP32_IR)
+    assert rep.status == bbpp.CONVERGED and rep.true_rel <= 1e-9 * 1.01
+    assert np.all(x[mask == 1] == 0)
+    assert np.abs(x - xo).max() <= 100 * 1e-9 * np.abs(xo).max()
